@@ -1,0 +1,976 @@
+// api.cu — host side of the C-ABI (include/arbo.h): parameter defaults, network and
+// community helpers, tables, device allocation, CUDA-graph step loop, data access.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/arbo.h"
+#include "sim_internal.h"
+
+using namespace arbo;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess) return fail(ARBO_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Human bi-Weibull CDF at an integer age (cpp/ndemographic.cu:13-29), in double, rounded once.
+float human_cdf(const arbo_sim_param& p, uint32_t a)
+{
+    double x = std::pow((double)a * (double)p.nScaleInfantMortality, (double)p.nShapeInfantMortality);
+    if ((double)a >= (double)p.nLocWeibull)
+        x += std::pow(((double)a - (double)p.nLocWeibull) / (double)p.nScaleLifeExpectancy,
+                      (double)p.nShapeLifeExpectancy);
+    return (float)(1.0 - std::exp(-x));
+}
+
+// Mosquito Weibull CDF (cpp/mdemographic.cu:13-17).
+float mosquito_cdf(const arbo_sim_param& p, uint32_t a)
+{
+    double x = std::pow((double)a / (double)p.mScaleLifeExpectancy, (double)p.mShapeLifeExpectancy);
+    return (float)(1.0 - std::exp(-x));
+}
+
+// CDF per integer age from 0 until it first reaches 1.0f (later ages read the last entry) or
+// until the oldest age the run can reach.
+std::vector<float> cdf_table(const arbo_sim_param& p, bool human, uint32_t max_age)
+{
+    std::vector<float> t;
+    t.reserve(std::min<uint32_t>(max_age + 1, 1u << 20));
+    for (uint32_t a = 0; a <= max_age; ++a) {
+        const float v = human ? human_cdf(p, a) : mosquito_cdf(p, a);
+        t.push_back(v);
+        if (v >= 1.0f) break;
+    }
+    return t;
+}
+
+float table_at(const std::vector<float>& t, uint32_t a) { return t[std::min<size_t>(a, t.size() - 1)]; }
+
+uint32_t comm_of_host(const std::vector<uint32_t>& loc, uint32_t P, uint32_t i)
+{
+    uint32_t lo = 0, hi = P;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (loc[mid] <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+}  // namespace
+
+struct arbo_sim {
+    Dev d{};
+    Launch l{};
+    arbo_sim_param p{};
+    arbo_arch_param arch{};
+    std::string odir;
+    uint32_t host_t = 0;
+    bool inited = false;
+    void* base = nullptr;
+    size_t bytes = 0;
+    std::vector<uint32_t> nsize, msize, nloc, mloc;
+    std::vector<float> etab;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t gmulti = nullptr, gone = nullptr;
+    uint32_t gsteps = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int device = 0;
+    uint64_t seed = 0;
+    uint32_t instance = 0;
+    uint64_t h2d = 0, d2h = 0;       // bytes copied by this handle
+    void* flush = nullptr;           // L2 flush buffer (measurement only)
+    size_t flush_bytes = 0;
+    std::vector<cudaEvent_t> step_ev;  // per-step event pairs of arbo_sim_time_steps
+};
+
+extern "C" {
+
+const char* arbo_last_error(void) { return g_err.c_str(); }
+
+const char* arbo_version(void) { return "arbo-gb300 0.1.0 (sm_103a)"; }
+
+int arbo_set_device(int device)
+{
+    CUDA_TRY(cudaSetDevice(device));
+    return ARBO_OK;
+}
+
+void arbo_sim_param_default(arbo_sim_param* p)
+{
+    std::memset(p, 0, sizeof(*p));
+    // SimulationParam::SimulationParam (cpp/SimulationParam.cpp:11-47).
+    p->nSize = 100000.0f;
+    p->metaPop = 10000.0f;
+    p->minMosToHuman = 1.5f;
+    p->mosNetGrowth = 0.5f;
+    p->nShapeInfantMortality = 0.4f;
+    p->nScaleInfantMortality = 1.0f / 100000.0f / 365.0f;
+    p->nScaleLifeExpectancy = 75.0f * 365.0f;
+    p->nShapeLifeExpectancy = 6.0f;
+    p->nLocWeibull = 8.0f * 365.0f;
+    p->mScaleLifeExpectancy = 23.0f;
+    p->mShapeLifeExpectancy = 4.0f;
+    p->netPower = 1.0f;
+    p->netM = 1.0f;
+    p->netSeed = 1.0f;
+    p->nHeteroPopSize = 0.0f;
+    p->mHeteroPopSize = 0.0f;
+    p->initialSeroPrev = 0.0f;
+    p->mInitialInf = 0.0f;
+    p->nInitialInf = 0.0f;
+    p->bitingRate = 0.25f;
+    p->mnBitingSuccess = 0.5f;
+    p->nmBitingSuccess = 0.5f;
+    p->recovery = 4.0f;
+    p->mExposed = 6.0f;
+    p->nExposed = 7.0f;
+    p->externalInfection = 5.0f;
+    p->longDistance = 0.01f;
+    p->exIncPeriodRange = 2.0f;
+    p->noDistance = 0.75f;
+    p->scaleCC = 1.0f;
+    // cpp/constant.h:8-28 as run-time values; mosquito slots as cpp/main.cpp:121 with scaleCC 1.
+    p->nStrains = 4;
+    p->mSize = (uint32_t)(p->minMosToHuman * 2.0f * p->nSize);
+    p->nMaxInitialAgeYears = 150;
+    p->mMaxInitialAge = 300;
+    p->maxIntroAttempt = 1000;
+    p->maxTargetAttempt = 1000;
+    p->quirks = ARBO_QUIRKS_REFERENCE;
+    p->recordSpatial = 0;
+    p->mosBaseRatio = 2.0f;
+    p->seasonAmp = 0.5f;
+    p->seasonPhase = 0.0f;
+}
+
+int arbo_arch_param_query(arbo_arch_param* a, int device)
+{
+    if (!a) return fail(ARBO_ERR_INVALID, "arbo_arch_param_query: null");
+    a->threadsPerWarp = 32;
+    a->totalSM = 152;
+    a->warpsPerSM = 64;
+    a->demogBlock = 256;
+    a->demogUnroll = 2;
+    a->foiBlock = 256;
+    a->infectBlock = 256;
+    a->graphSteps = 64;
+    int n = 0;
+    if (device >= 0 && cudaGetDeviceCount(&n) == cudaSuccess && device < n) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrWarpSize, device) == cudaSuccess) a->threadsPerWarp = (uint32_t)v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) == cudaSuccess) a->totalSM = (uint32_t)v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxThreadsPerMultiProcessor, device) == cudaSuccess)
+            a->warpsPerSM = (uint32_t)v / a->threadsPerWarp;
+    } else {
+        cudaGetLastError();
+    }
+    return ARBO_OK;
+}
+
+int arbo_lattice_csr(uint32_t side, uint32_t* loc, uint32_t* to, float* weight, uint32_t* nnz)
+{
+    if (side == 0 || !loc || !nnz) return fail(ARBO_ERR_INVALID, "arbo_lattice_csr: bad arguments");
+    // Node v = x + side*y (first coordinate fastest); rook neighbours, no wrap, no self loops.
+    uint32_t e = 0;
+    for (uint32_t y = 0; y < side; ++y) {
+        for (uint32_t x = 0; x < side; ++x) {
+            const uint32_t v = x + side * y;
+            loc[v] = e;
+            const uint32_t cand[4] = {y > 0 ? v - side : UINT32_MAX, x > 0 ? v - 1 : UINT32_MAX,
+                                      x + 1 < side ? v + 1 : UINT32_MAX, y + 1 < side ? v + side : UINT32_MAX};
+            for (int k = 0; k < 4; ++k) {
+                if (cand[k] == UINT32_MAX) continue;
+                if (to) to[e] = cand[k];
+                if (weight) weight[e] = 1.0f;
+                ++e;
+            }
+        }
+    }
+    loc[side * side] = e;
+    *nnz = e;
+    return ARBO_OK;
+}
+
+int arbo_cumulative_com_size(const uint32_t* loc, uint32_t P, float hetero, float* out)
+{
+    if (!loc || !out || P == 0) return fail(ARBO_ERR_INVALID, "arbo_cumulative_com_size: bad arguments");
+    std::vector<float> rel(P);
+    for (uint32_t c = 0; c < P; ++c) rel[c] = (float)std::pow((double)(loc[c + 1] - loc[c]), (double)hetero);
+    out[0] = rel[0];
+    for (uint32_t c = 1; c < P; ++c) out[c] = out[c - 1] + rel[c];
+    const float last = out[P - 1];
+    for (uint32_t c = 0; c < P; ++c) out[c] = out[c] / last;
+    return ARBO_OK;
+}
+
+int arbo_community_sizes(const double* w, uint32_t P, uint32_t total, uint32_t* out)
+{
+    if (!w || !out || P == 0) return fail(ARBO_ERR_INVALID, "arbo_community_sizes: bad arguments");
+    double sum = 0.0;
+    for (uint32_t c = 0; c < P; ++c) {
+        if (!(w[c] >= 0.0)) return fail(ARBO_ERR_INVALID, "arbo_community_sizes: negative or NaN weight");
+        sum += w[c];
+    }
+    if (!(sum > 0.0)) return fail(ARBO_ERR_INVALID, "arbo_community_sizes: weights sum to zero");
+    std::vector<double> frac(P);
+    uint64_t given = 0;
+    for (uint32_t c = 0; c < P; ++c) {
+        const double q = (double)total * w[c] / sum;
+        const double f = std::floor(q);
+        out[c] = (uint32_t)f;
+        frac[c] = q - f;
+        given += out[c];
+    }
+    std::vector<uint32_t> order(P);
+    for (uint32_t c = 0; c < P; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return frac[a] > frac[b]; });
+    uint64_t rem = total > given ? total - given : 0;
+    for (uint32_t k = 0; rem > 0; k = (k + 1) % P, --rem) out[order[k]] += 1;
+    return ARBO_OK;
+}
+
+int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const arbo_io_param* io, const arbo_csr* csr,
+                    const uint32_t* n_comm_size, const uint32_t* m_comm_size, uint32_t max_time, uint64_t seed,
+                    uint32_t instance, arbo_sim** out)
+{
+    if (!sp || !csr || !out) return fail(ARBO_ERR_INVALID, "arbo_sim_create: null argument");
+    *out = nullptr;
+    const arbo_sim_param& p = *sp;
+    const uint32_t P = csr->subPopTotal;
+    const uint32_t S = p.nStrains;
+    if (!(p.nSize >= 1.0f) || p.nSize > 2.0e9f) return fail(ARBO_ERR_INVALID, "nSize must be in [1, 2e9]");
+    const uint32_t N = (uint32_t)p.nSize;
+    const uint32_t M = p.mSize;
+    if (S < 1 || S > ARBO_MAX_STRAINS) return fail(ARBO_ERR_INVALID, "nStrains must be in [1, 8]");
+    if (P < 1 || (uint64_t)P * S >= (1ull << 28)) return fail(ARBO_ERR_INVALID, "subPopTotal out of range");
+    if (M < 1 || M > 2000000000u) return fail(ARBO_ERR_INVALID, "mSize must be in [1, 2e9]");
+    if (max_time < 1 || (uint64_t)max_time + 365ull * (p.nMaxInitialAgeYears + 1) > (1ull << 30))
+        return fail(ARBO_ERR_INVALID, "max_time out of range");
+    if (p.maxTargetAttempt < 1 || p.maxTargetAttempt > (1u << 18))
+        return fail(ARBO_ERR_INVALID, "maxTargetAttempt must be in [1, 2^18]");
+    if (p.maxIntroAttempt > (1u << 26)) return fail(ARBO_ERR_INVALID, "maxIntroAttempt must be <= 2^26");
+    if (!csr->loc || (csr->nnz && !csr->to) || csr->loc[0] != 0 || csr->loc[P] != csr->nnz)
+        return fail(ARBO_ERR_INVALID, "malformed CSR (loc[0] must be 0 and loc[P] == nnz)");
+    for (uint32_t c = 0; c < P; ++c)
+        if (csr->loc[c + 1] < csr->loc[c]) return fail(ARBO_ERR_INVALID, "malformed CSR: loc not ascending");
+    for (uint32_t e = 0; e < csr->nnz; ++e)
+        if (csr->to[e] >= P) return fail(ARBO_ERR_INVALID, "malformed CSR: column index out of range");
+    arbo_arch_param arch;
+    if (ap) arch = *ap; else arbo_arch_param_query(&arch, 0);
+    if (arch.demogBlock < 32 || arch.demogBlock > 512 || arch.demogBlock % 32 ||
+        !(arch.demogUnroll == 1 || arch.demogUnroll == 2 || arch.demogUnroll == 4) || arch.foiBlock < 32 ||
+        arch.foiBlock > 512 || arch.foiBlock % 32 || arch.infectBlock < 32 || arch.infectBlock > 512 ||
+        arch.infectBlock % 32)
+        return fail(ARBO_ERR_INVALID, "launch knobs: blocks must be multiples of 32 in [32, 512], unroll 1/2/4");
+
+    arbo_sim* s = new arbo_sim();
+    s->p = p;
+    s->arch = arch;
+    s->seed = seed;
+    s->instance = instance;
+    if (io && io->odir) s->odir = io->odir;
+    CUDA_TRY(cudaGetDevice(&s->device));
+
+    // Community sizes and contiguous census ranges.
+    s->nsize.resize(P);
+    s->msize.resize(P);
+    if (n_comm_size && m_comm_size) {
+        uint64_t sn = 0, sm = 0;
+        for (uint32_t c = 0; c < P; ++c) {
+            s->nsize[c] = n_comm_size[c];
+            s->msize[c] = m_comm_size[c];
+            sn += n_comm_size[c];
+            sm += m_comm_size[c];
+        }
+        if (sn != N || sm != M) {
+            delete s;
+            return fail(ARBO_ERR_INVALID, "community sizes must sum to nSize and mSize");
+        }
+    } else {
+        std::vector<double> wn(P), wm(P);
+        for (uint32_t c = 0; c < P; ++c) {
+            const double deg = (double)(csr->loc[c + 1] - csr->loc[c]);
+            wn[c] = std::pow(deg, (double)p.nHeteroPopSize);
+            wm[c] = std::pow(deg, (double)p.mHeteroPopSize);
+        }
+        if (arbo_community_sizes(wn.data(), P, N, s->nsize.data()) ||
+            arbo_community_sizes(wm.data(), P, M, s->msize.data())) {
+            delete s;
+            return ARBO_ERR_INVALID;
+        }
+    }
+    s->nloc.assign(P + 1, 0);
+    s->mloc.assign(P + 1, 0);
+    for (uint32_t c = 0; c < P; ++c) {
+        s->nloc[c + 1] = s->nloc[c] + s->nsize[c];
+        s->mloc[c + 1] = s->mloc[c] + s->msize[c];
+    }
+
+    // Tables.
+    const uint32_t T = max_time;
+    const std::vector<float> cdfh = cdf_table(p, true, 365u * p.nMaxInitialAgeYears + 364u + T + 1u);
+    const std::vector<float> cdfm = cdf_table(p, false, p.mMaxInitialAge + T + 1u);
+    std::vector<float> survh(p.nMaxInitialAgeYears + 1), survm(p.mMaxInitialAge + 1);
+    survh[0] = 1.0f - table_at(cdfh, 0);
+    for (uint32_t y = 1; y <= p.nMaxInitialAgeYears; ++y) survh[y] = survh[y - 1] + (1.0f - table_at(cdfh, 365u * y));
+    survm[0] = 1.0f - table_at(cdfm, 0);
+    for (uint32_t a = 1; a <= p.mMaxInitialAge; ++a) survm[a] = survm[a - 1] + (1.0f - table_at(cdfm, a));
+    s->etab.resize(T + 1);
+    for (uint32_t t = 0; t <= T; ++t) {
+        double e = (double)p.mosBaseRatio * (double)p.nSize *
+                   (1.0 + (double)p.seasonAmp * std::sin(2.0 * 3.14159265358979323846 * ((double)t - (double)p.seasonPhase) / 365.0));
+        e = std::min(e, (double)M);
+        e = std::max(e, 0.0);
+        s->etab[t] = (float)e;
+    }
+
+    Dev& d = s->d;
+    d.N = N;
+    d.M = M;
+    d.P = P;
+    d.S = S;
+    d.T = T;
+    d.nvec = (N + 3) / 4;
+    d.tiles = (M + kTile - 1) / kTile;
+    d.mvec = d.tiles * 32;
+    d.ah = (uint32_t)cdfh.size();
+    d.am = (uint32_t)cdfm.size();
+    d.yh = p.nMaxInitialAgeYears;
+    d.dm = p.mMaxInitialAge;
+    d.biting = p.bitingRate;
+    d.mnSuccess = p.mnBitingSuccess;
+    d.nmSuccess = p.nmBitingSuccess;
+    d.recovery = p.recovery;
+    d.mExposed = p.mExposed;
+    d.nExposed = p.nExposed;
+    d.extInf = p.externalInfection;
+    d.longDist = p.longDistance;
+    d.noDist = p.noDistance;
+    d.seroPrev = p.initialSeroPrev;
+    d.maxIntro = p.maxIntroAttempt;
+    d.maxTarget = p.maxTargetAttempt;
+    d.quirks = p.quirks;
+    d.recordSpatial = p.recordSpatial ? 1u : 0u;
+    d.nInit = std::min<uint32_t>((uint32_t)p.nInitialInf, N);
+    d.mInit = std::min<uint32_t>((uint32_t)p.mInitialInf, M);
+
+    // One allocation, every array 256-byte aligned.
+    const size_t Np = (size_t)d.nvec * 4, Mp = (size_t)d.tiles * kTile, SP = (size_t)S * P, R = (size_t)T + 1;
+    struct Item {
+        void** ptr;
+        size_t bytes;
+    };
+    std::vector<Item> items = {
+        {(void**)&d.n_age, Np * 4}, {(void**)&d.n_dage, Np * 4}, {(void**)&d.n_status, Np}, {(void**)&d.n_exposed, Np * 4},
+        {(void**)&d.n_recovery, Np * 4}, {(void**)&d.n_ple, Np * 4}, {(void**)&d.n_strain, Np}, {(void**)&d.n_imm, Np},
+        {(void**)&d.m_age, Mp * 4}, {(void**)&d.m_dage, Mp * 4}, {(void**)&d.m_state, Mp}, {(void**)&d.m_exposed, Mp * 4},
+        {(void**)&d.m_ple, Mp * 4}, {(void**)&d.m_strain, Mp}, {(void**)&d.ledger, (size_t)d.tiles * 4},
+        {(void**)&d.nloc, (P + 1) * 4}, {(void**)&d.mloc, (P + 1) * 4}, {(void**)&d.nsize, P * 4},
+        {(void**)&d.msize, P * 4}, {(void**)&d.tcomm, (size_t)d.tiles * 4}, {(void**)&d.csr_loc, (P + 1) * 4},
+        {(void**)&d.csr_to, std::max<size_t>(csr->nnz, 1) * 4}, {(void**)&d.infh, SP * 4}, {(void**)&d.infm, SP * 4},
+        {(void**)&d.inc, SP * 4}, {(void**)&d.ncnt, P * 4}, {(void**)&d.mcnt, P * 4}, {(void**)&d.transh, SP * 4},
+        {(void**)&d.transm, SP * 4}, {(void**)&d.cdfh, cdfh.size() * 4}, {(void**)&d.cdfm, cdfm.size() * 4},
+        {(void**)&d.survh, survh.size() * 4}, {(void**)&d.survm, survm.size() * 4}, {(void**)&d.etab, R * 4},
+        {(void**)&d.winh, Np * 8}, {(void**)&d.winm, Mp * 8}, {(void**)&d.s_ninc, R * S * 4},
+        {(void**)&d.s_ninf, R * S * 4}, {(void**)&d.s_one, R * S * 4}, {(void**)&d.s_ncount, R * 4},
+        {(void**)&d.s_mcount, R * 4}, {(void**)&d.s_minf, R * S * 4},
+        {(void**)&d.s_spatial, d.recordSpatial ? R * SP * 4 : 0}, {(void**)&d.ctrl, sizeof(Ctrl)},
+    };
+    size_t total = 0;
+    for (auto& it : items) total += align256(it.bytes);
+    cudaError_t ce = cudaMalloc(&s->base, total);
+    if (ce != cudaSuccess) {
+        delete s;
+        return fail(ARBO_ERR_ALLOC, std::string("cudaMalloc of the simulation (") + std::to_string(total) +
+                                        " bytes): " + cudaGetErrorString(ce));
+    }
+    s->bytes = total;
+    size_t off = 0;
+    for (auto& it : items) {
+        *it.ptr = it.bytes ? (void*)((char*)s->base + off) : nullptr;
+        off += align256(it.bytes);
+    }
+
+    std::vector<uint32_t> tcomm(d.tiles);
+    for (uint32_t b = 0; b < d.tiles; ++b) tcomm[b] = comm_of_host(s->mloc, P, b * kTile);
+    auto fail_free = [&](int code) {
+        arbo_sim_destroy(s);
+        return code;
+    };
+#define UP(dst, src, n)                                                                          \
+    do {                                                                                         \
+        cudaError_t e_ = cudaMemcpy((dst), (src), (n), cudaMemcpyHostToDevice);                  \
+        if (e_ != cudaSuccess) return fail_free(fail(ARBO_ERR_CUDA, cudaGetErrorString(e_)));    \
+        s->h2d += (n);                                                                           \
+    } while (0)
+    UP(d.nloc, s->nloc.data(), (P + 1) * 4);
+    UP(d.mloc, s->mloc.data(), (P + 1) * 4);
+    UP(d.nsize, s->nsize.data(), P * 4);
+    UP(d.msize, s->msize.data(), P * 4);
+    UP(d.ncnt, s->nsize.data(), P * 4);
+    UP(d.tcomm, tcomm.data(), (size_t)d.tiles * 4);
+    UP(d.csr_loc, csr->loc, (P + 1) * 4);
+    if (csr->nnz) UP(d.csr_to, csr->to, (size_t)csr->nnz * 4);
+    UP(d.cdfh, cdfh.data(), cdfh.size() * 4);
+    UP(d.cdfm, cdfm.data(), cdfm.size() * 4);
+    UP(d.survh, survh.data(), survh.size() * 4);
+    UP(d.survm, survm.data(), survm.size() * 4);
+    UP(d.etab, s->etab.data(), R * 4);
+    Ctrl c{};
+    c.k0 = (uint32_t)seed;
+    c.k1 = (uint32_t)(seed >> 32);
+    c.instance = instance;
+    UP(d.ctrl, &c, sizeof(Ctrl));
+#undef UP
+    if (cudaMemset(d.winh, 0xFF, Np * 8) != cudaSuccess || cudaMemset(d.winm, 0xFF, Mp * 8) != cudaSuccess ||
+        cudaMemset(d.transh, 0, SP * 4) != cudaSuccess || cudaMemset(d.transm, 0, SP * 4) != cudaSuccess)
+        return fail_free(fail(ARBO_ERR_CUDA, "cudaMemset at create"));
+
+    s->l.demogBlock = arch.demogBlock;
+    s->l.demogUnroll = arch.demogUnroll;
+    s->l.foiBlock = arch.foiBlock;
+    s->l.infectBlock = arch.infectBlock;
+    s->l.numSM = arch.totalSM;
+    if (cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess)
+        return fail_free(fail(ARBO_ERR_CUDA, "cudaStreamCreate"));
+    for (int k = 0; k < 4; ++k)
+        if (cudaEventCreate(&s->ev[k]) != cudaSuccess) return fail_free(fail(ARBO_ERR_CUDA, "cudaEventCreate"));
+    *out = s;
+    return ARBO_OK;
+}
+
+int arbo_sim_destroy(arbo_sim* s)
+{
+    if (!s) return ARBO_OK;
+    cudaSetDevice(s->device);
+    if (s->gmulti) cudaGraphExecDestroy(s->gmulti);
+    if (s->gone) cudaGraphExecDestroy(s->gone);
+    for (int k = 0; k < 4; ++k)
+        if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+    for (cudaEvent_t e : s->step_ev) cudaEventDestroy(e);
+    if (s->cap) cudaStreamDestroy(s->cap);
+    if (s->flush) cudaFree(s->flush);
+    if (s->base) cudaFree(s->base);
+    delete s;
+    return ARBO_OK;
+}
+
+int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* e, size_t n)
+{
+    if (!s || !e || n != (size_t)s->d.T + 1) return fail(ARBO_ERR_INVALID, "expected series must have max_time+1 entries");
+    CUDA_TRY(cudaSetDevice(s->device));
+    for (size_t t = 0; t < n; ++t) {
+        float v = e[t];
+        if (v > (float)s->d.M) v = (float)s->d.M;
+        if (!(v >= 0.0f)) v = 0.0f;
+        s->etab[t] = v;
+    }
+    CUDA_TRY(cudaMemcpy(s->d.etab, s->etab.data(), n * 4, cudaMemcpyHostToDevice));
+    s->h2d += n * 4;
+    return ARBO_OK;
+}
+
+int arbo_sim_set_seed(arbo_sim* s, uint64_t seed, uint32_t instance)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    CUDA_TRY(cudaSetDevice(s->device));
+    s->seed = seed;
+    s->instance = instance;
+    const uint32_t kv[3] = {(uint32_t)seed, (uint32_t)(seed >> 32), instance};
+    CUDA_TRY(cudaMemcpy(&s->d.ctrl->k0, kv, sizeof(kv), cudaMemcpyHostToDevice));
+    s->h2d += sizeof(kv);
+    return ARBO_OK;
+}
+
+int arbo_sim_init(arbo_sim* s, void* stream)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    CUDA_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const Dev& d = s->d;
+    const size_t SP = (size_t)d.S * d.P, R = (size_t)d.T + 1;
+    CUDA_TRY(cudaMemsetAsync(d.infh, 0, SP * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.infm, 0, SP * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.inc, 0, SP * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.transh, 0, SP * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.transm, 0, SP * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_ninc, 0, R * d.S * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_ninf, 0, R * d.S * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_one, 0, R * d.S * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_minf, 0, R * d.S * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_ncount, 0, R * 4, st));
+    CUDA_TRY(cudaMemsetAsync(d.s_mcount, 0, R * 4, st));
+    if (d.s_spatial) CUDA_TRY(cudaMemsetAsync(d.s_spatial, 0, R * SP * 4, st));
+    CUDA_TRY(cudaMemcpyAsync(d.mcnt, d.msize, (size_t)d.P * 4, cudaMemcpyDeviceToDevice, st));
+    const int e = launch_init(d, s->l, st);
+    if (e) return fail(ARBO_ERR_CUDA, std::string("init launch: ") + cudaGetErrorString((cudaError_t)e));
+    s->host_t = 0;
+    s->inited = true;
+    return ARBO_OK;
+}
+
+static int capture_graph(arbo_sim* s, uint32_t steps, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t k = 0; k < steps; ++k) {
+        const int e = launch_step(s->d, s->l, s->cap, nullptr);
+        if (e) {
+            cudaStreamEndCapture(s->cap, &g);
+            if (g) cudaGraphDestroy(g);
+            return fail(ARBO_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString((cudaError_t)e));
+        }
+    }
+    CUDA_TRY(cudaStreamEndCapture(s->cap, &g));
+    const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(ARBO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+    return ARBO_OK;
+}
+
+int arbo_sim_step(arbo_sim* s, uint32_t nsteps, void* stream)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    if (!s->inited) return fail(ARBO_ERR_STATE, "arbo_sim_step before arbo_sim_init");
+    CUDA_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t n = std::min(nsteps, s->d.T - s->host_t);
+    const uint32_t G = s->arch.graphSteps;
+    if (G == 0) {
+        for (uint32_t k = 0; k < n; ++k) {
+            const int e = launch_step(s->d, s->l, st, nullptr);
+            if (e) return fail(ARBO_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)e));
+            s->host_t += 1;
+        }
+        return ARBO_OK;
+    }
+    if (n >= G && !s->gmulti) {
+        const int e = capture_graph(s, G, &s->gmulti);
+        if (e) return e;
+    }
+    while (n >= G) {
+        CUDA_TRY(cudaGraphLaunch(s->gmulti, st));
+        n -= G;
+        s->host_t += G;
+    }
+    if (n > 0 && !s->gone) {
+        const int e = capture_graph(s, 1, &s->gone);
+        if (e) return e;
+    }
+    while (n > 0) {
+        CUDA_TRY(cudaGraphLaunch(s->gone, st));
+        n -= 1;
+        s->host_t += 1;
+    }
+    return ARBO_OK;
+}
+
+int arbo_sim_status(arbo_sim* s, void* stream, uint32_t* err_word, uint32_t* step)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    CUDA_TRY(cudaSetDevice(s->device));
+    Ctrl c;
+    CUDA_TRY(cudaMemcpyAsync(&c, s->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    s->d2h += sizeof(Ctrl);
+    if (err_word) *err_word = c.err;
+    if (step) *step = c.t;
+    return ARBO_OK;
+}
+
+int arbo_sim_run(arbo_sim* s, void* stream)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    int e = arbo_sim_step(s, s->d.T - s->host_t, stream);
+    if (e) return e;
+    uint32_t err = 0, t = 0;
+    e = arbo_sim_status(s, stream, &err, &t);
+    if (e) return e;
+    if (err) return fail(ARBO_ERR_DEVICE, "device error word set: " + std::to_string(err));
+    if (t != s->d.T) return fail(ARBO_ERR_STATE, "device step counter " + std::to_string(t) + " != " + std::to_string(s->d.T));
+    return ARBO_OK;
+}
+
+static int copy_out(arbo_sim* s, void* host, const void* dev, size_t bytes, void* stream)
+{
+    CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    s->d2h += bytes;
+    return ARBO_OK;
+}
+
+int arbo_sim_get_series(arbo_sim* s, arbo_series_kind kind, uint32_t* host, size_t n, void* stream)
+{
+    if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
+    const Dev& d = s->d;
+    const size_t R = (size_t)d.T + 1;
+    const uint32_t* src = nullptr;
+    size_t want = 0;
+    switch (kind) {
+    case ARBO_SERIES_N_INCIDENCE: src = d.s_ninc; want = R * d.S; break;
+    case ARBO_SERIES_N_INFECTED: src = d.s_ninf; want = R * d.S; break;
+    case ARBO_SERIES_ONE_SUBPOP: src = d.s_one; want = R * d.S; break;
+    case ARBO_SERIES_N_COUNT: src = d.s_ncount; want = R; break;
+    case ARBO_SERIES_M_COUNT: src = d.s_mcount; want = R; break;
+    case ARBO_SERIES_M_INFECTED: src = d.s_minf; want = R * d.S; break;
+    case ARBO_SERIES_INFECTED_SUBPOP:
+        if (!d.s_spatial) return fail(ARBO_ERR_STATE, "spatial series not recorded (recordSpatial = 0)");
+        src = d.s_spatial; want = R * d.S * d.P; break;
+    default: return fail(ARBO_ERR_INVALID, "unknown series kind");
+    }
+    if (n != want) return fail(ARBO_ERR_INVALID, "series length mismatch: expected " + std::to_string(want));
+    return copy_out(s, host, src, want * 4, stream);
+}
+
+static int counter_ptr(arbo_sim* s, arbo_counter_kind kind, void** ptr, size_t* n)
+{
+    const Dev& d = s->d;
+    const size_t SP = (size_t)d.S * d.P;
+    switch (kind) {
+    case ARBO_COUNTER_N_INFECTED_SUBPOP: *ptr = d.infh; *n = SP; break;
+    case ARBO_COUNTER_M_INFECTED_SUBPOP: *ptr = d.infm; *n = SP; break;
+    case ARBO_COUNTER_N_INCIDENCE_SUBPOP: *ptr = d.inc; *n = SP; break;
+    case ARBO_COUNTER_N_SUBPOP_COUNT: *ptr = d.ncnt; *n = d.P; break;
+    case ARBO_COUNTER_M_SUBPOP_COUNT: *ptr = d.mcnt; *n = d.P; break;
+    case ARBO_COUNTER_N_SUBPOP_LOC: *ptr = d.nloc; *n = (size_t)d.P + 1; break;
+    case ARBO_COUNTER_M_SUBPOP_LOC: *ptr = d.mloc; *n = (size_t)d.P + 1; break;
+    case ARBO_COUNTER_M_DEAD_COUNT: *ptr = d.ledger; *n = d.tiles; break;
+    case ARBO_COUNTER_DIAG: *ptr = d.ctrl->diag; *n = 4; break;
+    default: return fail(ARBO_ERR_INVALID, "unknown counter kind");
+    }
+    return ARBO_OK;
+}
+
+int arbo_sim_get_counters(arbo_sim* s, arbo_counter_kind kind, void* host, size_t n, void* stream)
+{
+    if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
+    void* ptr;
+    size_t want;
+    int e = counter_ptr(s, kind, &ptr, &want);
+    if (e) return e;
+    if (n != want) return fail(ARBO_ERR_INVALID, "counter length mismatch: expected " + std::to_string(want));
+    return copy_out(s, host, ptr, want * 4, stream);
+}
+
+int arbo_sim_set_counters(arbo_sim* s, arbo_counter_kind kind, const void* host, size_t n, void* stream)
+{
+    if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
+    if (kind == ARBO_COUNTER_N_SUBPOP_LOC || kind == ARBO_COUNTER_M_SUBPOP_LOC || kind == ARBO_COUNTER_DIAG)
+        return fail(ARBO_ERR_INVALID, "community ranges and diagnostics are read-only");
+    void* ptr;
+    size_t want;
+    int e = counter_ptr(s, kind, &ptr, &want);
+    if (e) return e;
+    if (n != want) return fail(ARBO_ERR_INVALID, "counter length mismatch: expected " + std::to_string(want));
+    CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaMemcpyAsync(ptr, host, want * 4, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    s->h2d += want * 4;
+    return ARBO_OK;
+}
+
+static int census_ptr(arbo_sim* s, arbo_census_field f, void** ptr, size_t* count, size_t* elem, int* packed)
+{
+    const Dev& d = s->d;
+    *packed = 0;
+    switch (f) {
+    case ARBO_CENSUS_N_AGE: *ptr = d.n_age; *elem = 4; break;
+    case ARBO_CENSUS_N_EXPOSED: *ptr = d.n_exposed; *elem = 4; break;
+    case ARBO_CENSUS_N_IMMUNITY: *ptr = d.n_imm; *elem = 1; break;
+    case ARBO_CENSUS_N_STATUS: *ptr = d.n_status; *elem = 1; break;
+    case ARBO_CENSUS_N_PLE: *ptr = d.n_ple; *elem = 4; break;
+    case ARBO_CENSUS_N_RECOVERY: *ptr = d.n_recovery; *elem = 4; break;
+    case ARBO_CENSUS_N_STRAIN: *ptr = d.n_strain; *elem = 1; break;
+    case ARBO_CENSUS_N_DEATH_AGE: *ptr = d.n_dage; *elem = 4; break;
+    case ARBO_CENSUS_M_AGE: *ptr = d.m_age; *elem = 4; break;
+    case ARBO_CENSUS_M_DEAD: *ptr = d.m_state; *elem = 1; *packed = 1; break;
+    case ARBO_CENSUS_M_EXPOSED: *ptr = d.m_exposed; *elem = 4; break;
+    case ARBO_CENSUS_M_STATUS: *ptr = d.m_state; *elem = 1; *packed = 2; break;
+    case ARBO_CENSUS_M_PLE: *ptr = d.m_ple; *elem = 4; break;
+    case ARBO_CENSUS_M_STRAIN: *ptr = d.m_strain; *elem = 1; break;
+    case ARBO_CENSUS_M_DEATH_AGE: *ptr = d.m_dage; *elem = 4; break;
+    default: return fail(ARBO_ERR_INVALID, "unknown census field");
+    }
+    *count = f <= ARBO_CENSUS_N_DEATH_AGE ? d.N : d.M;
+    return ARBO_OK;
+}
+
+int arbo_sim_get_census(arbo_sim* s, arbo_census_field f, void* host, size_t bytes, void* stream)
+{
+    if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
+    void* ptr;
+    size_t count, elem;
+    int packed;
+    int e = census_ptr(s, f, &ptr, &count, &elem, &packed);
+    if (e) return e;
+    if (bytes != count * elem) return fail(ARBO_ERR_INVALID, "census size mismatch: expected " + std::to_string(count * elem));
+    e = copy_out(s, host, ptr, bytes, stream);
+    if (e || !packed) return e;
+    uint8_t* h = (uint8_t*)host;
+    for (size_t i = 0; i < count; ++i) h[i] = packed == 1 ? (uint8_t)((h[i] & kDead) ? 1 : 0) : (uint8_t)(h[i] & 3u);
+    return ARBO_OK;
+}
+
+int arbo_sim_set_census(arbo_sim* s, arbo_census_field f, const void* host, size_t bytes, void* stream)
+{
+    if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
+    void* ptr;
+    size_t count, elem;
+    int packed;
+    int e = census_ptr(s, f, &ptr, &count, &elem, &packed);
+    if (e) return e;
+    if (bytes != count * elem) return fail(ARBO_ERR_INVALID, "census size mismatch: expected " + std::to_string(count * elem));
+    CUDA_TRY(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!packed) {
+        CUDA_TRY(cudaMemcpyAsync(ptr, host, bytes, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        s->h2d += bytes;
+        return ARBO_OK;
+    }
+    std::vector<uint8_t> cur(count);
+    e = copy_out(s, cur.data(), ptr, count, stream);
+    if (e) return e;
+    const uint8_t* h = (const uint8_t*)host;
+    for (size_t i = 0; i < count; ++i) {
+        if (packed == 1) cur[i] = (uint8_t)((cur[i] & 3u) | (h[i] ? kDead : 0u));
+        else cur[i] = (uint8_t)((cur[i] & kDead) | (h[i] & 3u));
+    }
+    CUDA_TRY(cudaMemcpyAsync(ptr, cur.data(), count, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    s->h2d += count;
+    return ARBO_OK;
+}
+
+int arbo_sim_dims(const arbo_sim* s, uint32_t* n, uint32_t* m, uint32_t* p, uint32_t* strains, uint32_t* max_time,
+                  uint32_t* tiles)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    if (n) *n = s->d.N;
+    if (m) *m = s->d.M;
+    if (p) *p = s->d.P;
+    if (strains) *strains = s->d.S;
+    if (max_time) *max_time = s->d.T;
+    if (tiles) *tiles = s->d.tiles;
+    return ARBO_OK;
+}
+
+static int ensure_flush(arbo_sim* s, uint32_t flush_mb)
+{
+    const size_t want = (size_t)flush_mb << 20;
+    if (want == 0 || s->flush_bytes >= want) return ARBO_OK;
+    if (s->flush) cudaFree(s->flush);
+    s->flush = nullptr;
+    s->flush_bytes = 0;
+    CUDA_TRY(cudaMalloc(&s->flush, want + 256));
+    CUDA_TRY(cudaMemset(s->flush, 0, want + 256));
+    s->flush_bytes = want;
+    return ARBO_OK;
+}
+
+static int flush_l2(arbo_sim* s, uint32_t flush_mb, cudaStream_t st)
+{
+    if (!flush_mb) return ARBO_OK;
+    const int e = launch_l2_flush(s->flush, (size_t)flush_mb << 20, (uint32_t*)((char*)s->flush + s->flush_bytes),
+                                  s->l.numSM, st);
+    return e ? fail(ARBO_ERR_CUDA, std::string("flush launch: ") + cudaGetErrorString((cudaError_t)e)) : ARBO_OK;
+}
+
+int arbo_sim_time_phases(arbo_sim* s, uint32_t nsteps, uint32_t flush_mb, float* ms_out, void* stream)
+{
+    if (!s || !ms_out) return fail(ARBO_ERR_INVALID, "null argument");
+    if (!s->inited) return fail(ARBO_ERR_STATE, "arbo_sim_time_phases before arbo_sim_init");
+    CUDA_TRY(cudaSetDevice(s->device));
+    int e = ensure_flush(s, flush_mb);
+    if (e) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t n = std::min(nsteps, s->d.T - s->host_t);
+    double acc[4] = {0, 0, 0, 0};
+    for (uint32_t k = 0; k < n; ++k) {
+        if ((e = flush_l2(s, flush_mb, st))) return e;
+        e = launch_step(s->d, s->l, st, s->ev);
+        if (e) return fail(ARBO_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)e));
+        s->host_t += 1;
+        CUDA_TRY(cudaEventSynchronize(s->ev[3]));
+        float a = 0, b = 0, c = 0, w = 0;
+        CUDA_TRY(cudaEventElapsedTime(&a, s->ev[0], s->ev[1]));
+        CUDA_TRY(cudaEventElapsedTime(&b, s->ev[1], s->ev[2]));
+        CUDA_TRY(cudaEventElapsedTime(&c, s->ev[2], s->ev[3]));
+        CUDA_TRY(cudaEventElapsedTime(&w, s->ev[0], s->ev[3]));
+        acc[0] += a;
+        acc[1] += b;
+        acc[2] += c;
+        acc[3] += w;
+    }
+    for (int k = 0; k < 4; ++k) ms_out[k] = n ? (float)(acc[k] / n) : 0.0f;
+    return ARBO_OK;
+}
+
+// A graph of `steps` steps, each preceded by the optional L2 flush and bracketed by its own
+// pair of external event-record nodes.
+static int capture_timed(arbo_sim* s, uint32_t steps, uint32_t flush_mb, cudaGraphExec_t* out)
+{
+    while (s->step_ev.size() < 2 * (size_t)steps) {
+        cudaEvent_t e;
+        CUDA_TRY(cudaEventCreate(&e));
+        s->step_ev.push_back(e);
+    }
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    int err = ARBO_OK;
+    for (uint32_t k = 0; k < steps && !err; ++k) {
+        if ((err = flush_l2(s, flush_mb, s->cap))) break;
+        if (cudaEventRecordWithFlags(s->step_ev[2 * k], s->cap, cudaEventRecordExternal) != cudaSuccess) {
+            err = fail(ARBO_ERR_CUDA, "event record in capture");
+            break;
+        }
+        const int e = launch_step(s->d, s->l, s->cap, nullptr);
+        if (e) {
+            err = fail(ARBO_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString((cudaError_t)e));
+            break;
+        }
+        if (cudaEventRecordWithFlags(s->step_ev[2 * k + 1], s->cap, cudaEventRecordExternal) != cudaSuccess)
+            err = fail(ARBO_ERR_CUDA, "event record in capture");
+    }
+    const cudaError_t ce = cudaStreamEndCapture(s->cap, &g);
+    if (err) {
+        if (g) cudaGraphDestroy(g);
+        return err;
+    }
+    if (ce != cudaSuccess) return fail(ARBO_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(ARBO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+    return ARBO_OK;
+}
+
+int arbo_sim_time_steps(arbo_sim* s, uint32_t nsteps, uint32_t flush_mb, float* step_ms, void* stream)
+{
+    if (!s || !step_ms) return fail(ARBO_ERR_INVALID, "null argument");
+    if (!s->inited) return fail(ARBO_ERR_STATE, "arbo_sim_time_steps before arbo_sim_init");
+    CUDA_TRY(cudaSetDevice(s->device));
+    int e = ensure_flush(s, flush_mb);
+    if (e) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t n = std::min(nsteps, s->d.T - s->host_t);
+    for (uint32_t k = n; k < nsteps; ++k) step_ms[k] = 0.0f;
+    const uint32_t G = std::max<uint32_t>(1, std::min<uint32_t>(s->arch.graphSteps ? s->arch.graphSteps : 1, 64));
+    cudaGraphExec_t full = nullptr;
+    uint32_t done = 0;
+    while (done < n) {
+        const uint32_t chunk = std::min(G, n - done);
+        cudaGraphExec_t ex = nullptr;
+        if (chunk == G && full) {
+            ex = full;
+        } else {
+            if ((e = capture_timed(s, chunk, flush_mb, &ex))) {
+                if (full) cudaGraphExecDestroy(full);
+                return e;
+            }
+            if (chunk == G) full = ex;
+        }
+        cudaError_t ce = cudaGraphLaunch(ex, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        for (uint32_t k = 0; k < chunk && ce == cudaSuccess; ++k)
+            ce = cudaEventElapsedTime(&step_ms[done + k], s->step_ev[2 * k], s->step_ev[2 * k + 1]);
+        if (ex != full) cudaGraphExecDestroy(ex);
+        if (ce != cudaSuccess) {
+            if (full) cudaGraphExecDestroy(full);
+            return fail(ARBO_ERR_CUDA, std::string("timed steps: ") + cudaGetErrorString(ce));
+        }
+        done += chunk;
+        s->host_t += chunk;
+    }
+    if (full) cudaGraphExecDestroy(full);
+    return ARBO_OK;
+}
+
+int arbo_sim_io_bytes(const arbo_sim* s, uint64_t* h2d, uint64_t* d2h)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    if (h2d) *h2d = s->h2d;
+    if (d2h) *d2h = s->d2h;
+    return ARBO_OK;
+}
+
+uint32_t arbo_sim_launches_per_step(const arbo_sim* s)
+{
+    (void)s;
+    return launches_per_step();
+}
+
+int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, void* stream)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    if (s->odir.empty()) return fail(ARBO_ERR_INVALID, "io->odir not set");
+    const uint32_t S = s->d.S, T = s->d.T;
+    std::vector<uint32_t> inc((size_t)(T + 1) * S), inf((size_t)(T + 1) * S), one((size_t)(T + 1) * S), cnt(T + 1);
+    int e;
+    if ((e = arbo_sim_get_series(s, ARBO_SERIES_N_INCIDENCE, inc.data(), inc.size(), stream)) ||
+        (e = arbo_sim_get_series(s, ARBO_SERIES_N_INFECTED, inf.data(), inf.size(), stream)) ||
+        (e = arbo_sim_get_series(s, ARBO_SERIES_ONE_SUBPOP, one.data(), one.size(), stream)) ||
+        (e = arbo_sim_get_series(s, ARBO_SERIES_N_COUNT, cnt.data(), cnt.size(), stream)))
+        return e;
+    // writeIncidence (cpp/writeoutput.cpp:13-98): header on the first replicate, rows t = 0..T.
+    const std::string path = s->odir + "/nData" + std::to_string(mcmc_run) + ".csv";
+    FILE* f = std::fopen(path.c_str(), sim_run == 0 ? "w" : "a");
+    if (!f) return fail(ARBO_ERR_INVALID, "cannot open " + path);
+    if (sim_run == 0) {
+        std::fprintf(f, "t,popSize");
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",incidence_DENV%u", k + 1);
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",prevalence_DENV%u", k + 1);
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",prevalence_DENV%u_random_community", k + 1);
+        std::fprintf(f, ",simRun");
+    }
+    for (uint32_t t = 0; t <= T; ++t) {
+        std::fprintf(f, "\n%u,%u", t, cnt[t]);
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",%u", inc[(size_t)t * S + k]);
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",%u", inf[(size_t)t * S + k]);
+        for (uint32_t k = 0; k < S; ++k) std::fprintf(f, ",%u", one[(size_t)t * S + k]);
+        std::fprintf(f, ",%u", sim_run);
+    }
+    std::fclose(f);
+    return ARBO_OK;
+}
+
+int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, void* stream)
+{
+    if (!s || !out) return fail(ARBO_ERR_INVALID, "null argument");
+    const uint32_t S = s->d.S, T = s->d.T;
+    std::vector<uint32_t> inc((size_t)(T + 1) * S);
+    int e = arbo_sim_get_series(s, ARBO_SERIES_N_INCIDENCE, inc.data(), inc.size(), stream);
+    if (e) return e;
+    // MCMC::storeIncidence (cpp/MCMC.cpp:190-213): week w sums the days 7w..7w+6 that exist.
+    for (uint32_t w = 0; w < max_week; ++w) {
+        uint64_t acc = 0;
+        for (uint32_t k = 0; k < 7; ++k) {
+            const uint64_t t = 7ull * w + k;
+            if (t > T) break;
+            for (uint32_t q = 0; q < S; ++q) acc += inc[t * S + q];
+        }
+        out[w] = (uint32_t)acc;
+    }
+    return ARBO_OK;
+}
+
+}  // extern "C"

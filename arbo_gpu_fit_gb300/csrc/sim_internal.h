@@ -1,0 +1,113 @@
+// sim_internal.h — device-side layout of one simulation and the kernel launchers.
+//
+// Layout in HBM (structure of arrays, every array 256-byte aligned, one allocation):
+//   humans   (N padded to a multiple of 4 agents):  age i32, death_age i32, status u8,
+//            exposed i32, recovery i32, ple f32, strain u8, immunity u8.
+//   mosquito (M padded to whole 128-slot tiles):     age i32, death_age i32, state u8
+//            (bits 0-1 status, bit 7 dead), exposed i32, ple f32, strain u8; tile dead
+//            count i32 per tile.
+//   The census is community-sorted: community c owns the contiguous index range
+//   [loc[c], loc[c+1]) of each species, so infection draws hit contiguous ranges and a
+//   128-slot tile spans one or two communities.
+//   counters [S*P] u32: infected humans, infectious mosquitoes, human incidence, events on
+//            humans, events on mosquitoes; [P] humans and alive mosquitoes per community.
+//   tables:  CDF per integer age (human, mosquito), yearly/daily survival sums, E[M_t].
+//   winners: u64 per agent, (~epoch << 32 | serial order) of the first eligible event.
+//   series:  (T+1) rows of the recorded time series.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "philox.cuh"
+
+namespace arbo {
+
+constexpr uint8_t kPad = 0xFF;        // status byte of a padding agent
+constexpr uint8_t kDead = 0x80;       // mosquito state: dead flag
+constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
+constexpr uint32_t kMaxEventsPerPair = 1u << 24;
+
+struct Ctrl {
+    uint32_t t;          // current step
+    uint32_t epoch;      // steps taken since the handle was created (winner tags)
+    uint32_t err;        // ARBO_DEVERR_* bits
+    uint32_t done;       // CTAs finished in the infection kernel of this step
+    uint32_t diag[4];    // dropped mosquito events, exhausted introductions, -, -
+    uint32_t k0, k1;     // random key (seed low / high word)
+    uint32_t instance;   // 16-bit stream id of this simulation
+    uint32_t pad;
+};
+
+struct Dev {
+    // dimensions
+    uint32_t N, M, P, S, T, tiles, nvec, mvec;
+    uint32_t ah, am, yh, dm;
+    // parameters
+    float biting, mnSuccess, nmSuccess, recovery, mExposed, nExposed, extInf, longDist, noDist, seroPrev;
+    uint32_t maxIntro, maxTarget, quirks, recordSpatial, nInit, mInit;
+    // humans
+    int32_t* n_age;
+    int32_t* n_dage;
+    uint8_t* n_status;
+    int32_t* n_exposed;
+    int32_t* n_recovery;
+    float* n_ple;
+    uint8_t* n_strain;
+    uint8_t* n_imm;
+    // mosquitoes
+    int32_t* m_age;
+    int32_t* m_dage;
+    uint8_t* m_state;
+    int32_t* m_exposed;
+    float* m_ple;
+    uint8_t* m_strain;
+    int32_t* ledger;
+    // communities and network
+    uint32_t* nloc;   // [P+1]
+    uint32_t* mloc;   // [P+1]
+    uint32_t* nsize;  // [P]
+    uint32_t* msize;  // [P]
+    uint32_t* tcomm;  // [tiles] community of each mosquito tile's first slot
+    uint32_t* csr_loc;
+    uint32_t* csr_to;
+    // counters
+    uint32_t* infh;
+    uint32_t* infm;
+    uint32_t* inc;
+    uint32_t* ncnt;
+    uint32_t* mcnt;
+    uint32_t* transh;  // events acting on humans   [S*P]
+    uint32_t* transm;  // events acting on mosquitoes [S*P]
+    // tables
+    float* cdfh;
+    float* cdfm;
+    float* survh;
+    float* survm;
+    float* etab;
+    // winners
+    unsigned long long* winh;
+    unsigned long long* winm;
+    // series
+    uint32_t* s_ninc;
+    uint32_t* s_ninf;
+    uint32_t* s_one;
+    uint32_t* s_ncount;
+    uint32_t* s_mcount;
+    uint32_t* s_minf;
+    uint32_t* s_spatial;
+    Ctrl* ctrl;
+};
+
+struct Launch {
+    uint32_t demogBlock, demogUnroll, foiBlock, infectBlock, numSM;
+};
+
+// Kernel launchers (kernels.cu). Each returns the cudaError_t of the launch as int.
+int launch_init(const Dev& d, const Launch& l, void* stream);
+// One time step; with events != null, records cudaEvent_t events[0..3] around the three kernels.
+int launch_step(const Dev& d, const Launch& l, void* stream, void* events);
+uint32_t launches_per_step();
+// Reads `bytes` of buf (a multiple of 16) to evict L2; `sink` is a device word never written in practice.
+int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_sm, cudaStream_t st);
+
+}  // namespace arbo

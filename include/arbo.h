@@ -1,0 +1,341 @@
+/*
+ * arbo.h — C-ABI of the GB300-native (sm_103a) per-time-step dengue agent simulation.
+ *
+ * Plain C: POD structs, plain pointers and sizes, an int status (ARBO_OK == 0), no CUDA
+ * or torch types (a stream is passed as `void*`, i.e. a cudaStream_t or NULL for the
+ * legacy default stream). Every entry point below replaces one piece of the reference's
+ * host API (wtennant/arbo_gpu_fit, directory cpp/); the replaced symbol is cited as
+ * file:line beside each declaration.
+ *
+ * Ownership: the library owns the census, the counters and the time series of a
+ * simulation handle (the reference's caller cudaMalloc'd ~50 buffers per MCMC step,
+ * cpp/main.cpp:198-249). The caller keeps ownership of every pointer it passes in; the
+ * library copies what it needs before returning.
+ *
+ * Threading: one handle per host thread, or external synchronisation. All device work
+ * of a call is issued on the stream given to that call.
+ *
+ * Errors: a non-zero return code; arbo_last_error() returns the text of the last error
+ * raised on the calling thread. No C++ exception crosses this boundary.
+ */
+#ifndef ARBO_H
+#define ARBO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define ARBO_OK 0
+#define ARBO_ERR_INVALID 1  /* bad argument or parameter                     */
+#define ARBO_ERR_CUDA 2     /* a CUDA runtime call failed                     */
+#define ARBO_ERR_ALLOC 3    /* device or host allocation failed               */
+#define ARBO_ERR_DEVICE 4   /* a kernel raised the device error word          */
+#define ARBO_ERR_STATE 5    /* call out of order (e.g. step before init)      */
+
+/* Bits of the device error word (arbo_sim_status). */
+#define ARBO_DEVERR_EVENT_OVERFLOW 0x1u /* > 2^24 events for one (strain, community) in a step */
+#define ARBO_DEVERR_COUNTER 0x2u        /* a counter would have gone below zero               */
+
+#define ARBO_MAX_STRAINS 8u
+#define ARBO_MOSQUITO_TILE 128u /* logical recruitment tile (reference C_THREADSPERBLOCK) */
+
+/* Model switches that reproduce documented behaviours of the reference. */
+#define ARBO_QUIRK_SEED_RECOVERY_DURATION 0x1u /* cpp/epidemicinitial.cu:62-63: seed recovery is a
+                                                  duration compared with an age (seeds recover at
+                                                  once) */
+#define ARBO_QUIRK_SEED_DEAD_MOSQUITO 0x2u     /* cpp/epidemicinitial.cu:89-97: mosquito seeds may
+                                                  land on dead slots and stay counted */
+#define ARBO_QUIRKS_REFERENCE 0x3u
+
+/* ------------------------------------------------------------------ parameters */
+
+/*
+ * arbo_sim_param — replaces class SimulationParam (cpp/SimulationParam.h:12-60), whose
+ * field order and meaning the first 33 members keep. The trailing members are the
+ * compile-time constants of cpp/constant.h:8-28 turned into run-time values, plus the
+ * seasonal mosquito target that replaces the climate-driven logistic update of
+ * cpp/simulation.cpp:83-88,129-132.
+ */
+typedef struct arbo_sim_param {
+    /* Demographic parameters (cpp/SimulationParam.h:16-26). */
+    float nSize;                 /* humans in the metapopulation                         */
+    float metaPop;               /* communities                                          */
+    float minMosToHuman;         /* unused by the seasonal target (kept for shape)       */
+    float mosNetGrowth;          /* unused by the seasonal target (kept for shape)       */
+    float nShapeInfantMortality; /* human bi-Weibull, first term: (a*scale)^shape        */
+    float nScaleInfantMortality;
+    float nScaleLifeExpectancy;  /* human bi-Weibull, second term ((a-loc)/scale)^shape  */
+    float nShapeLifeExpectancy;
+    float nLocWeibull;           /* age (days) at which the second term starts           */
+    float mScaleLifeExpectancy;  /* mosquito Weibull (a/scale)^shape                     */
+    float mShapeLifeExpectancy;
+    /* Network generation (cpp/SimulationParam.h:29-33). */
+    float netPower;
+    float netM;
+    float netSeed;
+    float nHeteroPopSize;        /* community size weight = degree^nHeteroPopSize        */
+    float mHeteroPopSize;
+    /* Epidemiology (cpp/SimulationParam.h:36-48). */
+    float initialSeroPrev;       /* probability of prior immunity to each serotype       */
+    float mInitialInf;           /* initially infectious mosquitoes (count)              */
+    float nInitialInf;           /* initially infectious humans (count)                  */
+    float bitingRate;
+    float mnBitingSuccess;       /* mosquito -> human transmission probability per bite  */
+    float nmBitingSuccess;       /* human -> mosquito transmission probability per bite  */
+    float recovery;              /* human infectious period (days)                       */
+    float mExposed;              /* mosquito extrinsic incubation period (days)          */
+    float nExposed;              /* human latent period (days)                           */
+    float externalInfection;     /* imported infections per day per serotype             */
+    float longDistance;          /* fraction of dispersed events sent uniformly at random */
+    float exIncPeriodRange;      /* unused (climate)                                     */
+    float noDistance;            /* fraction of events that stay in the source community */
+    /* Climate scaling (cpp/SimulationParam.h:51-54): unused without climate input. */
+    float scaleEIP;
+    float scaleMLE;
+    float scaleCC;
+    float scaleHumidity;
+
+    /* Run-time forms of cpp/constant.h and the seasonal mosquito target. */
+    uint32_t nStrains;           /* C_STRAINS, 1..8                                       */
+    uint32_t mSize;              /* mosquito slots                                        */
+    uint32_t nMaxInitialAgeYears;/* C_NMAXINITIALAGE (150)                                */
+    uint32_t mMaxInitialAge;     /* C_MMAXINITIALAGE (300)                                */
+    uint32_t maxIntroAttempt;    /* C_MAXINTROATTEMPT (1000)                              */
+    uint32_t maxTargetAttempt;   /* cap on dead-slot retries of one mosquito event        */
+    uint32_t quirks;             /* ARBO_QUIRK_* bits                                     */
+    uint32_t recordSpatial;      /* 1: keep the per-community infected series            */
+    float mosBaseRatio;          /* E[M_t] = mosBaseRatio*nSize*(1+seasonAmp*sin(2*pi*(t-seasonPhase)/365)) */
+    float seasonAmp;
+    float seasonPhase;
+    float reserved0;
+} arbo_sim_param;
+
+/*
+ * arbo_arch_param — replaces ArchitectureParam (cpp/ArchitectureParam.h:8-15). The three
+ * device fields keep their meaning; the rest are launch-shape knobs. Results do not depend
+ * on any knob (the random stream is keyed by entity, not by thread).
+ */
+typedef struct arbo_arch_param {
+    uint32_t threadsPerWarp;
+    uint32_t warpsPerSM;
+    uint32_t totalSM;
+    uint32_t demogBlock;     /* threads per CTA of the demographic kernel (multiple of 32) */
+    uint32_t demogUnroll;    /* 4-agent groups per thread (1, 2 or 4)                      */
+    uint32_t foiBlock;       /* threads per CTA of the force-of-infection kernel           */
+    uint32_t infectBlock;    /* threads per CTA of the infection kernel                    */
+    uint32_t graphSteps;     /* steps captured per CUDA graph (0: no graph)                */
+} arbo_arch_param;
+
+/* arbo_io_param — replaces IOParam (cpp/IOParam.h:10-25). Only odir is used (CSV output). */
+typedef struct arbo_io_param {
+    const char* idir;
+    const char* iClimateFile;
+    const char* iDengueFile;
+    const char* odir;
+} arbo_io_param;
+
+/*
+ * arbo_csr — the dispersal network in compressed sparse row form, the format of
+ * igraphSparseToCSR (cpp/network.cpp:76-114): loc[subPopTotal+1] row starts, to[nnz]
+ * column (destination community) indices ascending within a row, weight[nnz].
+ * Weights are carried but, as in the reference, the destination is drawn uniformly over
+ * a row (cpp/nepidemic.cu:101-116).
+ */
+typedef struct arbo_csr {
+    uint32_t subPopTotal;
+    uint32_t nnz;
+    const uint32_t* loc;
+    const uint32_t* to;
+    const float* weight;
+} arbo_csr;
+
+typedef struct arbo_sim arbo_sim; /* opaque simulation handle */
+
+/* Time series recorded once per step (cpp/datacollect.cu:10-74, cpp/main.cpp:225-235). */
+typedef enum arbo_series_kind {
+    ARBO_SERIES_N_INCIDENCE = 0,      /* d_nIncidence [(T+1)*S]                          */
+    ARBO_SERIES_N_INFECTED = 1,       /* d_nInfectedCount [(T+1)*S]                      */
+    ARBO_SERIES_ONE_SUBPOP = 2,       /* d_nOneSubPopInfectedCount [(T+1)*S] (community 0) */
+    ARBO_SERIES_N_COUNT = 3,          /* d_nCount [T+1]                                  */
+    ARBO_SERIES_M_COUNT = 4,          /* d_mCount [T+1]                                  */
+    ARBO_SERIES_M_INFECTED = 5,       /* infectious mosquitoes per serotype [(T+1)*S]    */
+    ARBO_SERIES_INFECTED_SUBPOP = 6   /* d_nInfectedSubPopCountSeries [(T+1)*S*P]        */
+} arbo_series_kind;
+
+/* Per-(serotype, community) and per-community counters (cpp/main.cpp:216-246). */
+typedef enum arbo_counter_kind {
+    ARBO_COUNTER_N_INFECTED_SUBPOP = 0, /* d_nInfectedSubPopCount [S*P] */
+    ARBO_COUNTER_M_INFECTED_SUBPOP = 1, /* d_mInfectedSubPopCount [S*P] */
+    ARBO_COUNTER_N_INCIDENCE_SUBPOP = 2,/* d_nIncidenceSubPop [S*P]     */
+    ARBO_COUNTER_N_SUBPOP_COUNT = 3,    /* d_nSubPopCount [P]           */
+    ARBO_COUNTER_M_SUBPOP_COUNT = 4,    /* d_mSubPopCount [P]           */
+    ARBO_COUNTER_N_SUBPOP_LOC = 5,      /* d_nSubPopLoc [P+1] (range starts) */
+    ARBO_COUNTER_M_SUBPOP_LOC = 6,      /* d_mSubPopLoc [P+1]           */
+    ARBO_COUNTER_M_DEAD_COUNT = 7,      /* d_mDeadCount per 128-slot tile [ceil(M/128)] (int32) */
+    ARBO_COUNTER_DIAG = 8               /* [4] u32: dropped mosquito events, exhausted intros (lo, hi), steps */
+} arbo_counter_kind;
+
+/* Census fields (cpp/censustypedef.h:8-16 with the widths of this build). */
+typedef enum arbo_census_field {
+    ARBO_CENSUS_N_AGE = 0,        /* int32 [N] days                                   */
+    ARBO_CENSUS_N_EXPOSED = 1,    /* int32 [N] age at which infection becomes infectious */
+    ARBO_CENSUS_N_IMMUNITY = 2,   /* uint8 [N] bit s = immune to serotype s (history != -1) */
+    ARBO_CENSUS_N_STATUS = 3,     /* uint8 [N] 0 susceptible, 1 infected, 2 infectious */
+    ARBO_CENSUS_N_PLE = 4,        /* float [N] life-expectancy probability            */
+    ARBO_CENSUS_N_RECOVERY = 5,   /* int32 [N] age at which infection ends            */
+    ARBO_CENSUS_N_STRAIN = 6,     /* uint8 [N]                                        */
+    ARBO_CENSUS_N_DEATH_AGE = 7,  /* int32 [N] first age whose CDF reaches PLE        */
+    ARBO_CENSUS_M_AGE = 8,        /* int32 [M]                                        */
+    ARBO_CENSUS_M_DEAD = 9,       /* uint8 [M] 1 = dead slot                          */
+    ARBO_CENSUS_M_EXPOSED = 10,   /* int32 [M]                                        */
+    ARBO_CENSUS_M_STATUS = 11,    /* uint8 [M]                                        */
+    ARBO_CENSUS_M_PLE = 12,       /* float [M]                                        */
+    ARBO_CENSUS_M_STRAIN = 13,    /* uint8 [M]                                        */
+    ARBO_CENSUS_M_DEATH_AGE = 14  /* int32 [M]                                        */
+} arbo_census_field;
+
+/* ------------------------------------------------------------------ host helpers */
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* arbo_last_error(void);
+
+/* Library version string. */
+const char* arbo_version(void);
+
+/* Make `device` the current CUDA device of the calling host thread for this library (handles
+ * created afterwards live there). The reference always used device 0 (cpp/ArchitectureParam.cpp:14-23). */
+int arbo_set_device(int device);
+
+/* Default parameters: SimulationParam::SimulationParam (cpp/SimulationParam.cpp:11-47)
+ * plus the cpp/constant.h values (C_STRAINS promoted to 4). */
+void arbo_sim_param_default(arbo_sim_param* p);
+
+/* Device geometry and default launch knobs: ArchitectureParam::ArchitectureParam
+ * (cpp/ArchitectureParam.cpp:9-24). device < 0 or no GPU: fills GB300 figures. */
+int arbo_arch_param_query(arbo_arch_param* a, int device);
+
+/* Non-periodic side x side rook lattice in CSR form, rows and columns ascending, weights
+ * 1.0: replaces createNetwork (lattice branch) + igraphSparseToCSR (cpp/network.cpp:29-46,
+ * 76-114). loc has side*side+1 entries; to/weight need capacity 4*side*(side-1).
+ * *nnz receives the number of entries. */
+int arbo_lattice_csr(uint32_t side, uint32_t* loc, uint32_t* to, float* weight, uint32_t* nnz);
+
+/* Normalised cumulative community-size weights degree^hetero: calcCumulativeComSize
+ * (cpp/network.cpp:119-164). out has subPopTotal entries, the last equal to 1. */
+int arbo_cumulative_com_size(const uint32_t* loc, uint32_t subPopTotal, float hetero, float* out);
+
+/* Integer community sizes summing exactly to total, proportional to weights (largest
+ * remainder, ties to the lower index). The build assigns each community a contiguous
+ * census range of this size (the reference's subPopIndex, cpp/demographicintial.cu:367-406). */
+int arbo_community_sizes(const double* weights, uint32_t subPopTotal, uint32_t total, uint32_t* out);
+
+/* ------------------------------------------------------------------ simulation */
+
+/*
+ * Create a simulation handle: allocates the census, counters, tables and time series on
+ * the current device, uploads the network and community sizes. Replaces the allocation
+ * and upload block of main (cpp/main.cpp:198-259).
+ *   n_comm_size / m_comm_size: humans / mosquito slots per community (P entries each,
+ *     summing to nSize / mSize). NULL: sizes proportional to calcCumulativeComSize's
+ *     degree^hetero weights (cpp/network.cpp:119-164).
+ *   max_time: steps of one run (the reference's maxTime); series hold max_time+1 rows.
+ *   instance: 16-bit stream id mixed into every random draw (0 for a single run).
+ */
+int arbo_sim_create(const arbo_sim_param* sim, const arbo_arch_param* arch, const arbo_io_param* io,
+                    const arbo_csr* csr, const uint32_t* n_comm_size, const uint32_t* m_comm_size,
+                    uint32_t max_time, uint64_t seed, uint32_t instance, arbo_sim** out);
+
+/* Release every device and host resource of the handle (cpp/main.cpp:284-335). */
+int arbo_sim_destroy(arbo_sim* s);
+
+/* Replace the expected mosquito population series E[0..max_time] (n = max_time+1 floats,
+ * host memory). Default: the seasonal target of arbo_sim_param. Replaces the host array
+ * h_mExpectedPopSize of cpp/simulation.cpp:84-132. Values above mSize are capped. */
+int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* expected, size_t n);
+
+/* Re-seed the handle (next arbo_sim_init uses it). */
+int arbo_sim_set_seed(arbo_sim* s, uint64_t seed, uint32_t instance);
+
+/* Initialise census, counters and series and record series row 0: replaces setupCudaRNG
+ * + demographicInitialization + epidemicInitial + dataCollect(0) (cpp/simulation.cpp:87-120,
+ * cpp/setuprng.cu:27-40, cpp/demographicintial.cu:411-486, cpp/epidemicinitial.cu:135-185). */
+int arbo_sim_init(arbo_sim* s, void* stream);
+
+/* Advance nsteps time steps: per step the human and mosquito demographic passes, the
+ * series row of the next time point, the force of infection with dispersal, and the
+ * infection draws. Replaces the body of the time loop of simulation (cpp/simulation.cpp:
+ * 115-155): nDemographic, mDemographic, epidemic, dataCollect. Asynchronous on `stream`. */
+int arbo_sim_step(arbo_sim* s, uint32_t nsteps, void* stream);
+
+/* Run the remaining steps up to max_time and synchronise; returns ARBO_ERR_DEVICE if the
+ * device error word is set. Replaces simulation (cpp/simulation.cpp:18-191) minus the file
+ * output. */
+int arbo_sim_run(arbo_sim* s, void* stream);
+
+/* Synchronise `stream` and read the device error word (ARBO_DEVERR_* bits) and the
+ * current step. */
+int arbo_sim_status(arbo_sim* s, void* stream, uint32_t* err_word, uint32_t* step);
+
+/* Copy a time series to host memory (n elements of uint32). Synchronises the stream. */
+int arbo_sim_get_series(arbo_sim* s, arbo_series_kind kind, uint32_t* host, size_t n, void* stream);
+
+/* Copy a counter array to host memory (n elements of 4 bytes). */
+int arbo_sim_get_counters(arbo_sim* s, arbo_counter_kind kind, void* host, size_t n, void* stream);
+
+/* Copy / overwrite a census field (bytes = element count * element size). Setting a field
+ * does not update the counters; arbo_sim_set_counters does. Test and resume hooks. */
+int arbo_sim_get_census(arbo_sim* s, arbo_census_field field, void* host, size_t bytes, void* stream);
+int arbo_sim_set_census(arbo_sim* s, arbo_census_field field, const void* host, size_t bytes, void* stream);
+int arbo_sim_set_counters(arbo_sim* s, arbo_counter_kind kind, const void* host, size_t n, void* stream);
+
+/* Sizes of the handle: N, M, P, S, T, tiles. Any pointer may be NULL. */
+int arbo_sim_dims(const arbo_sim* s, uint32_t* n, uint32_t* m, uint32_t* p, uint32_t* strains,
+                  uint32_t* max_time, uint32_t* tiles);
+
+/* Run nsteps steps kernel by kernel (no graph) with CUDA events between the kernels on
+ * `stream`, and return the mean duration in ms of each kernel in ms_out[4]:
+ * [0] demographic, [1] force of infection + series, [2] infection draws, [3] whole step.
+ * flush_mb > 0: before each step (outside the timed interval) a kernel reads a flush_mb MiB
+ * buffer so that the step starts with a cold L2. No reference counterpart (measurement). */
+int arbo_sim_time_phases(arbo_sim* s, uint32_t nsteps, uint32_t flush_mb, float* ms_out, void* stream);
+
+/* Run nsteps steps as captured CUDA graphs, each step bracketed by its own pair of CUDA
+ * events on `stream`, and write each step's duration in ms to step_ms[nsteps]. flush_mb as in
+ * arbo_sim_time_phases. No reference counterpart (measurement). */
+int arbo_sim_time_steps(arbo_sim* s, uint32_t nsteps, uint32_t flush_mb, float* step_ms, void* stream);
+
+/* Bytes copied host->device and device->host by this handle since it was created. */
+int arbo_sim_io_bytes(const arbo_sim* s, uint64_t* h2d, uint64_t* d2h);
+
+/* Number of kernel launches one step issues (for launch accounting). */
+uint32_t arbo_sim_launches_per_step(const arbo_sim* s);
+
+/* Append the time series of this run in the reference's nData<mcmcRun>.csv format
+ * (writeIncidence, cpp/writeoutput.cpp:13-98) under io->odir. */
+int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, void* stream);
+
+/* Weekly incidence of serotype-summed daily incidence: MCMC::storeIncidence
+ * (cpp/MCMC.cpp:190-213) — week w sums days 7w..7w+6 that exist (<= max_time).
+ * out has max_week entries. */
+int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, void* stream);
+
+/* ------------------------------------------------------------------ self-tests */
+
+/* Evaluate the device Philox4x32-10 on n (counter[4], key[2]) records packed as 6 uint32 each
+ * (host memory in/out; out has 4*n entries). No reference counterpart: checks that the device
+ * random stream equals the host restatement. */
+int arbo_selftest_philox(const uint32_t* ctr_key, uint32_t n, uint32_t* out);
+
+/* The first n outputs (4*n uint32) of curand's Philox4_32_10 generator for curand_init(seed, 0, 0),
+ * computed on the device. No reference counterpart: a library cross-check of the Philox rounds. */
+int arbo_selftest_curand_philox(uint64_t seed, uint32_t n, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARBO_H */
