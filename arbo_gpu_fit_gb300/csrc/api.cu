@@ -276,11 +276,12 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         if (csr->to[e] >= P) return fail(ARBO_ERR_INVALID, "malformed CSR: column index out of range");
     arbo_arch_param arch;
     if (ap) arch = *ap; else arbo_arch_param_query(&arch, 0);
-    if (arch.demogBlock < 32 || arch.demogBlock > 512 || arch.demogBlock % 32 ||
+    if (arch.demogBlock < 32 || arch.demogBlock > 256 || arch.demogBlock % 32 ||
         !(arch.demogUnroll == 1 || arch.demogUnroll == 2 || arch.demogUnroll == 4) || arch.foiBlock < 32 ||
         arch.foiBlock > 512 || arch.foiBlock % 32 || arch.infectBlock < 32 || arch.infectBlock > 512 ||
         arch.infectBlock % 32)
-        return fail(ARBO_ERR_INVALID, "launch knobs: blocks must be multiples of 32 in [32, 512], unroll 1/2/4");
+        return fail(ARBO_ERR_INVALID, "launch knobs: demogBlock in [32, 256], foiBlock and infectBlock in [32, 512], "
+                                      "all multiples of 32; demogUnroll 1, 2 or 4");
 
     arbo_sim* s = new arbo_sim();
     s->p = p;
@@ -329,6 +330,13 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     const uint32_t T = max_time;
     const std::vector<float> cdfh = cdf_table(p, true, 365u * p.nMaxInitialAgeYears + 364u + T + 1u);
     const std::vector<float> cdfm = cdf_table(p, false, p.mMaxInitialAge + T + 1u);
+    std::vector<uint32_t> minv(4098);
+    for (uint32_t k = 0, a = 0; k <= 4096; ++k) {
+        const float thr = (float)k / 4096.0f;
+        while (a < cdfm.size() && cdfm[a] < thr) ++a;
+        minv[k] = a;
+    }
+    minv[4097] = (uint32_t)cdfm.size();
     std::vector<float> survh(p.nMaxInitialAgeYears + 1), survm(p.mMaxInitialAge + 1);
     survh[0] = 1.0f - table_at(cdfh, 0);
     for (uint32_t y = 1; y <= p.nMaxInitialAgeYears; ++y) survh[y] = survh[y - 1] + (1.0f - table_at(cdfh, 365u * y));
@@ -388,7 +396,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         {(void**)&d.msize, P * 4}, {(void**)&d.tcomm, (size_t)d.tiles * 4}, {(void**)&d.csr_loc, (P + 1) * 4},
         {(void**)&d.csr_to, std::max<size_t>(csr->nnz, 1) * 4}, {(void**)&d.infh, SP * 4}, {(void**)&d.infm, SP * 4},
         {(void**)&d.inc, SP * 4}, {(void**)&d.ncnt, P * 4}, {(void**)&d.mcnt, P * 4}, {(void**)&d.transh, SP * 4},
-        {(void**)&d.transm, SP * 4}, {(void**)&d.cdfh, cdfh.size() * 4}, {(void**)&d.cdfm, cdfm.size() * 4},
+        {(void**)&d.transm, SP * 4}, {(void**)&d.cdfh, cdfh.size() * 4}, {(void**)&d.cdfm, cdfm.size() * 4}, {(void**)&d.minv, minv.size() * 4},
         {(void**)&d.survh, survh.size() * 4}, {(void**)&d.survm, survm.size() * 4}, {(void**)&d.etab, R * 4},
         {(void**)&d.winh, Np * 8}, {(void**)&d.winm, Mp * 8}, {(void**)&d.s_ninc, R * S * 4},
         {(void**)&d.s_ninf, R * S * 4}, {(void**)&d.s_one, R * S * 4}, {(void**)&d.s_ncount, R * 4},
@@ -432,6 +440,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     if (csr->nnz) UP(d.csr_to, csr->to, (size_t)csr->nnz * 4);
     UP(d.cdfh, cdfh.data(), cdfh.size() * 4);
     UP(d.cdfm, cdfm.data(), cdfm.size() * 4);
+    UP(d.minv, minv.data(), minv.size() * 4);
     UP(d.survh, survh.data(), survh.size() * 4);
     UP(d.survm, survm.data(), survm.size() * 4);
     UP(d.etab, s->etab.data(), R * 4);
@@ -450,6 +459,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     s->l.foiBlock = arch.foiBlock;
     s->l.infectBlock = arch.infectBlock;
     s->l.numSM = arch.totalSM;
+    s->l.demogBlocksPerSM = (uint32_t)demog_blocks_per_sm(arch.demogUnroll, arch.demogBlock);
     if (cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess)
         return fail_free(fail(ARBO_ERR_CUDA, "cudaStreamCreate"));
     for (int k = 0; k < 4; ++k)
@@ -532,8 +542,8 @@ static int capture_graph(arbo_sim* s, uint32_t steps, cudaGraphExec_t* out)
 {
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
-    for (uint32_t k = 0; k < steps; ++k) {
-        const int e = launch_step(s->d, s->l, s->cap, nullptr);
+    for (uint32_t k = 0; k <= steps; ++k) {
+        const int e = k < steps ? launch_step(s->d, s->l, s->cap, nullptr, k) : launch_advance(s->d, steps, s->cap);
         if (e) {
             cudaStreamEndCapture(s->cap, &g);
             if (g) cudaGraphDestroy(g);
@@ -557,7 +567,8 @@ int arbo_sim_step(arbo_sim* s, uint32_t nsteps, void* stream)
     const uint32_t G = s->arch.graphSteps;
     if (G == 0) {
         for (uint32_t k = 0; k < n; ++k) {
-            const int e = launch_step(s->d, s->l, st, nullptr);
+            int e = launch_step(s->d, s->l, st, nullptr, 0);
+            if (!e) e = launch_advance(s->d, 1, st);
             if (e) return fail(ARBO_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)e));
             s->host_t += 1;
         }
@@ -808,7 +819,8 @@ int arbo_sim_time_phases(arbo_sim* s, uint32_t nsteps, uint32_t flush_mb, float*
     double acc[4] = {0, 0, 0, 0};
     for (uint32_t k = 0; k < n; ++k) {
         if ((e = flush_l2(s, flush_mb, st))) return e;
-        e = launch_step(s->d, s->l, st, s->ev);
+        e = launch_step(s->d, s->l, st, s->ev, 0);
+        if (!e) e = launch_advance(s->d, 1, st);
         if (e) return fail(ARBO_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)e));
         s->host_t += 1;
         CUDA_TRY(cudaEventSynchronize(s->ev[3]));
@@ -844,13 +856,17 @@ static int capture_timed(arbo_sim* s, uint32_t steps, uint32_t flush_mb, cudaGra
             err = fail(ARBO_ERR_CUDA, "event record in capture");
             break;
         }
-        const int e = launch_step(s->d, s->l, s->cap, nullptr);
+        const int e = launch_step(s->d, s->l, s->cap, nullptr, k);
         if (e) {
             err = fail(ARBO_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString((cudaError_t)e));
             break;
         }
         if (cudaEventRecordWithFlags(s->step_ev[2 * k + 1], s->cap, cudaEventRecordExternal) != cudaSuccess)
             err = fail(ARBO_ERR_CUDA, "event record in capture");
+    }
+    if (!err) {
+        const int e = launch_advance(s->d, steps, s->cap);
+        if (e) err = fail(ARBO_ERR_CUDA, std::string("advance capture: ") + cudaGetErrorString((cudaError_t)e));
     }
     const cudaError_t ce = cudaStreamEndCapture(s->cap, &g);
     if (err) {
@@ -916,7 +932,7 @@ int arbo_sim_io_bytes(const arbo_sim* s, uint64_t* h2d, uint64_t* d2h)
 uint32_t arbo_sim_launches_per_step(const arbo_sim* s)
 {
     (void)s;
-    return launches_per_step();
+    return launches_per_step();  // plus one step-counter launch per captured graph
 }
 
 int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, void* stream)

@@ -182,180 +182,294 @@ __device__ __forceinline__ uint32_t slot_comm(const Dev& d, uint32_t c0, uint32_
 }
 
 // Rare per-mosquito counter change (death of an infectious mosquito, or E->I).
-__device__ __noinline__ void mosq_counter(uint32_t* infm, const uint8_t* m_strain, const uint32_t* mloc, uint32_t P,
-                                          uint32_t c0, uint32_t i, int add, Ctrl* ctrl)
+__device__ __noinline__ void mosq_counter(uint32_t* infm, const uint8_t* m_strain, const uint32_t* __restrict__ mloc,
+                                          const uint32_t* __restrict__ tcomm, uint32_t P, uint32_t i, int add, Ctrl* ctrl)
 {
-    uint32_t c = c0;
+    uint32_t c = __ldg(&tcomm[i / kTile]);
     while (c + 1 < P && __ldg(&mloc[c + 1]) <= i) ++c;
     uint32_t* p = &infm[m_strain[i] * P + c];
     if (add > 0) atomicAdd(p, 1u); else counter_dec(p, ctrl);
 }
 
-template <int U>
-__device__ __forceinline__ void demog_mosquitoes(const Dev& d, const Key key, uint32_t w0, uint32_t wstride,
-                                                 uint32_t lane, uint32_t t)
+// First age whose mosquito CDF reaches ple, via the inverse bucket table: with
+// j = floor(ple * 4096), minv[j] (first age with CDF >= j/4096) and minv[j+1] bracket the
+// answer, so a short binary search between them is exact. minv[4097] = table size (none).
+__device__ __forceinline__ int32_t death_age_m(const float* __restrict__ cdf, const uint32_t* __restrict__ minv,
+                                               uint32_t n, float ple)
 {
-    uint32_t SW[U];
-    int4 A[U], D[U];
+    const uint32_t j = (uint32_t)(ple * 4096.0f);
+    uint32_t lo = __ldg(&minv[j]), hi = __ldg(&minv[j + 1]);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&cdf[mid]) >= ple) hi = mid; else lo = mid + 1;
+    }
+    return lo >= n ? INT_MAX : (int32_t)lo;
+}
+
+constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
+
+// Bit 7 of each byte of x gathered into a 4-bit mask (byte k -> bit k).
+__device__ __forceinline__ uint32_t nibble7(uint32_t x)
+{
+    return (((x >> 7) & 0x01010101u) * 0x01020408u) >> 24;
+}
+
+__device__ __forceinline__ uint32_t pick4(const U4& v, uint32_t i)
+{
+    return i == 0 ? v.v[0] : i == 1 ? v.v[1] : i == 2 ? v.v[2] : v.v[3];
+}
+
+// Per-warp shared staging of the mosquito pass: reborn slot offsets by rank and the Philox
+// outputs of the groups of four reborn slots, for the four tiles of a quad.
+struct QuadSmem {
+    uint4 draw[kQuad][32];
+    uint8_t slot[kQuad][kTile];
+};
+
+// The m lowest set bits of a 4-bit mask, from 64-bit tables of sixteen 4-bit entries.
+__host__ __device__ constexpr uint32_t keep_low_bits(uint32_t mask, uint32_t m)
+{
+    uint32_t out = 0;
+    for (uint32_t b = 0; b < 4; ++b)
+        if (((mask >> b) & 1u) && m > 0) {
+            out |= 1u << b;
+            --m;
+        }
+    return out;
+}
+__host__ __device__ constexpr unsigned long long keep_low_table(uint32_t m)
+{
+    unsigned long long v = 0;
+    for (uint32_t mask = 0; mask < 16; ++mask) v |= (unsigned long long)keep_low_bits(mask, m) << (4 * mask);
+    return v;
+}
+__device__ __forceinline__ uint32_t keep_low(uint32_t mask, uint32_t m)
+{
+    constexpr unsigned long long L1 = keep_low_table(1), L2 = keep_low_table(2), L3 = keep_low_table(3);
+    if (m == 0) return 0u;
+    if (m >= 4) return mask;
+    const unsigned long long lut = m == 1 ? L1 : m == 2 ? L2 : L3;
+    return (uint32_t)(lut >> (4 * mask)) & 0xFu;
+}
+
+// One warp, tiles 4q..4q+3; lane l holds slots 4l..4l+3 of each tile. Per tile: ageing and
+// deaths, the birth quota (cpp/mdemographic.cu:104-129) from the carried dead count, rebirth of
+// the lowest-index dead slots, the net change of each community's alive count. The quota draws
+// of the four tiles come from one Philox call; the r-th reborn slot of tile b takes component
+// r&3 of the call keyed (b, t, r>>2). Per-tile counts of the four tiles travel packed in the
+// four bytes of one word (at most 128 per tile), so one warp reduction or scan serves all four.
+// Slot-owner lanes age their slots, store the aged ages, clear the state bytes of their reborn
+// slots and post each reborn slot's offset under its rank; one lane per group of four reborn
+// slots then draws the group, and one lane per reborn slot writes the newborn's age, PLE and
+// death age.
+__device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key, uint32_t q, uint32_t lane, uint32_t t,
+                                                    QuadSmem& sm)
+{
+    const uint32_t b0 = q * kQuad;
+    uint32_t SW[kQuad];
+    int4 A[kQuad], D[kQuad];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const uint32_t b = w0 + u * wstride;
-        if (b < d.tiles) {
-            const uint32_t g = b * 32 + lane;
+    for (uint32_t u = 0; u < kQuad; ++u) {
+        if (b0 + u < d.tiles) {
+            const uint32_t g = (b0 + u) * 32 + lane;
             SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.m_state) + g);
             A[u] = reinterpret_cast<const int4*>(d.m_age)[g];
-            D[u] = reinterpret_cast<const int4*>(d.m_dage)[g];
+            D[u] = __ldcs(reinterpret_cast<const int4*>(d.m_dage) + g);
+        } else {
+            SW[u] = 0xFFFFFFFFu;
+            A[u] = make_int4(0, 0, 0, 0);
+            D[u] = A[u];
         }
     }
-    const float E = __ldg(&d.etab[t + 1]);
+    const uint32_t bl = b0 + lane;
+    const bool tile_lane = lane < kQuad && bl < d.tiles;
+    const int32_t led = tile_lane ? d.ledger[bl] : 0;
+    const uint32_t cl = tile_lane ? __ldg(&d.tcomm[bl]) : 0u;
+    const uint32_t cl_end = tile_lane ? __ldg(&d.mloc[cl + 1]) : 0u;
+    const U4 rq = draw4(key, kMosquitoTile, q, t);
+
+    uint32_t deadm = 0, diedm = 0;  // 4 bits per tile
+    uint32_t chg = 0;               // bit u: state word of tile u changed
+    uint32_t ndp = 0, diedp = 0;    // packed per-tile counts of this lane: dead after deaths, died now
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-        const uint32_t b = w0 + u * wstride;
-        if (b >= d.tiles) continue;  // warp-uniform
-        const uint32_t g = b * 32 + lane;
-        const uint32_t c0 = __ldg(&d.tcomm[b]);
-        int32_t a[4] = {A[u].x, A[u].y, A[u].z, A[u].w};
-        int32_t dd[4] = {D[u].x, D[u].y, D[u].z, D[u].w};
+    for (uint32_t u = 0; u < kQuad; ++u) {
         const uint32_t sw = SW[u];
-        uint32_t nsw = sw;
-        uint32_t deaths = 0, deadmask = 0;
-        int net[4] = {0, 0, 0, 0};
-        bool aged = false;
+        // Byte-parallel masks of the four state bytes (bit 7 of a byte: dead or padding).
+        const uint32_t alive4 = ~sw & 0x80808080u;
+        const uint32_t pad4 = __vcmpeq4(sw, 0xFFFFFFFFu);
+        const uint32_t dead4 = sw & 0x80808080u & ~pad4;
+        int32_t a[4] = {A[u].x + (int32_t)((alive4 >> 7) & 1u), A[u].y + (int32_t)((alive4 >> 15) & 1u),
+                        A[u].z + (int32_t)((alive4 >> 23) & 1u), A[u].w + (int32_t)(alive4 >> 31)};
+        uint32_t dim = 0;
+        dim |= ((alive4 & 0x00000080u) && a[0] >= D[u].x) ? 1u : 0u;
+        dim |= ((alive4 & 0x00008000u) && a[1] >= D[u].y) ? 2u : 0u;
+        dim |= ((alive4 & 0x00800000u) && a[2] >= D[u].z) ? 4u : 0u;
+        dim |= ((alive4 & 0x80000000u) && a[3] >= D[u].w) ? 8u : 0u;
+        const uint32_t dm = nibble7(dead4) | dim;
+        const uint32_t stat4 = sw & 0x03030303u;
+        uint32_t rm = nibble7(((stat4 | (stat4 >> 1)) & (alive4 >> 7)) << 7);
+        uint32_t ns = sw | (((dim * 0x00204081u) & 0x01010101u) << 7);
+        const uint32_t g = (b0 + u) * 32 + lane;
+        if (alive4) reinterpret_cast<int4*>(d.m_age)[g] = make_int4(a[0], a[1], a[2], a[3]);
+        // Rare: deaths of infectious mosquitoes and latent-to-infectious transitions.
+        while (rm) {
+            const int k = __ffs(rm) - 1;
+            rm &= rm - 1;
+            const uint32_t i = 4 * g + k;
+            const uint32_t st = (ns >> (8 * k)) & 0xFFu;
+            if (st & kDead) {
+                if ((st & 3u) == 2u) mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, -1, d.ctrl);
+            } else if ((st & 3u) == 1u) {
+                const int32_t ak = k == 0 ? a[0] : k == 1 ? a[1] : k == 2 ? a[2] : a[3];
+                if (d.m_exposed[i] < ak) {
+                    ns = (ns & ~(0x3u << (8 * k))) | (2u << (8 * k));
+                    mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, +1, d.ctrl);
+                }
+            }
+        }
+        if (ns != sw) chg |= 1u << u;
+        SW[u] = ns;
+        deadm |= dm << (4 * u);
+        diedm |= dim << (4 * u);
+        ndp |= (uint32_t)__popc(dm) << (8 * u);
+        diedp |= (uint32_t)__popc(dim) << (8 * u);
+    }
+    // Deaths per tile (packed) and the birth quotas: lane u computes tile b0+u.
+    const uint32_t died_all = __reduce_add_sync(kFull, diedp);
+    int births_l = 0;
+    if (tile_lane) {
+        const uint32_t start = bl * kTile;
+        const uint32_t bt = (d.M - start) < kTile ? (d.M - start) : kTile;
+        const uint32_t L = (uint32_t)led + ((died_all >> (8 * lane)) & 0xFFu);
+        const float fbt = (float)bt;
+        float x = __fmul_rn(__ldg(&d.etab[t + 1]), fbt);
+        x = __fdiv_rn(x, (float)d.M);
+        x = __fsub_rn(x, fbt);
+        x = __fadd_rn(x, (float)L);
+        births_l = (int)resolve(x, pick4(rq, lane));
+        d.ledger[bl] = (int32_t)L - births_l;
+    }
+    // Ranks of dead slots (slot order): packed exclusive scan of the per-lane dead counts.
+    uint32_t incl = ndp;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= (uint32_t)off) incl += y;
+    }
+    const uint32_t excl = incl - ndp;
+    const uint32_t tot = __shfl_sync(kFull, incl, 31);
+    uint32_t bornp = 0, nb_pack = 0, gtot = 0, gst = 0;
+#pragma unroll
+    for (uint32_t u = 0; u < kQuad; ++u) {
+        const int bu = __shfl_sync(kFull, births_l, u);
+        const uint32_t total = (tot >> (8 * u)) & 0xFFu;
+        const uint32_t nb = (bu > 0 && b0 + u < d.tiles) ? min((uint32_t)bu, total) : 0u;
+        nb_pack |= nb << (8 * u);
+        gst |= gtot << (8 * u);
+        gtot += (nb + 3) >> 2;
+        const uint32_t pre = (excl >> (8 * u)) & 0xFFu;
+        const uint32_t dm = (deadm >> (4 * u)) & 0xFu;
+        const uint32_t born = keep_low(dm, nb > pre ? nb - pre : 0u);
+        if (born) {
+            uint32_t bm = born, r = pre;
+            while (bm) {
+                const int k = __ffs(bm) - 1;
+                bm &= bm - 1;
+                sm.slot[u][r++] = (uint8_t)(4 * lane + k);
+            }
+            SW[u] &= ~(((born * 0x00204081u) & 0x01010101u) * 0xFFu);
+        }
+        if (born || ((chg >> u) & 1u)) reinterpret_cast<unsigned int*>(d.m_state)[(b0 + u) * 32 + lane] = SW[u];
+        bornp |= (uint32_t)__popc(born) << (8 * u);
+    }
+    // Alive count per community: one atomic per tile when the tile lies in one community.
+    const uint32_t born_all = __reduce_add_sync(kFull, bornp);
+    const bool single_l = tile_lane && cl_end >= min((bl + 1) * kTile, d.M);
+    if (single_l) {
+        const int net = (int)((born_all >> (8 * lane)) & 0xFFu) - (int)((died_all >> (8 * lane)) & 0xFFu);
+        if (net != 0) atomicAdd(&d.mcnt[cl], (unsigned)net);
+    }
+    const unsigned single = __ballot_sync(kFull, single_l);
+#pragma unroll
+    for (uint32_t u = 0; u < kQuad; ++u) {
+        if (b0 + u >= d.tiles || ((single >> u) & 1u)) continue;  // warp-uniform
+        const uint32_t g = (b0 + u) * 32 + lane;
+        const uint32_t c0 = __ldg(&d.tcomm[b0 + u]);
+        const uint32_t dim = (diedm >> (4 * u)) & 0xFu;
+        const uint32_t pre = (excl >> (8 * u)) & 0xFFu, nb = (nb_pack >> (8 * u)) & 0xFFu;
+        const uint32_t born = keep_low((deadm >> (4 * u)) & 0xFu, nb > pre ? nb - pre : 0u);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            uint32_t st = (sw >> (8 * k)) & 0xFFu;
-            if (st == kPad) continue;
-            if (st & kDead) {
-                deadmask |= 1u << k;
-                continue;
-            }
-            aged = true;
-            a[k] += 1;
-            if (a[k] >= dd[k]) {
-                if ((st & 3u) == 2u) mosq_counter(d.infm, d.m_strain, d.mloc, d.P, c0, 4 * g + k, -1, d.ctrl);
-                st |= kDead;
-                deadmask |= 1u << k;
-                deaths += 1;
-                net[k] = -1;
-            } else if ((st & 3u) == 1u) {
-                if (d.m_exposed[4 * g + k] < a[k]) {
-                    st = (st & ~3u) | 2u;
-                    mosq_counter(d.infm, d.m_strain, d.mloc, d.P, c0, 4 * g + k, +1, d.ctrl);
-                }
-            }
-            nsw = (nsw & ~(0xFFu << (8 * k))) | (st << (8 * k));
-        }
-        // Birth quota of the tile (cpp/mdemographic.cu:104-129), from the carried dead count.
-        const uint32_t tile_deaths = __reduce_add_sync(kFull, deaths);
-        int births = 0;
-        if (lane == 0) {
-            const uint32_t start = b * kTile;
-            const uint32_t bt = (d.M - start) < kTile ? (d.M - start) : kTile;
-            const uint32_t L = (uint32_t)d.ledger[b] + tile_deaths;
-            const float fbt = (float)bt;
-            float x = __fmul_rn(E, fbt);
-            x = __fdiv_rn(x, (float)d.M);
-            x = __fsub_rn(x, fbt);
-            x = __fadd_rn(x, (float)L);
-            const U4 r = draw4(key, kMosquitoTile, b, t);
-            births = (int)resolve(x, r.v[0]);
-            d.ledger[b] = (int32_t)L - births;
-        }
-        births = __shfl_sync(kFull, births, 0);
-        // Rebirth of the lowest-index dead slots of the tile: rank = dead slots before this one.
-        const uint32_t ndead = __popc(deadmask);
-        uint32_t incl = ndead;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t v = __shfl_up_sync(kFull, incl, off);
-            if (lane >= (uint32_t)off) incl += v;
-        }
-        int rank = (int)(incl - ndead);
-        bool reborn = false;
-        if (deadmask != 0 && rank < births) {
-            const U4 r = draw4(key, kMosquitoRebirth, g, t);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!((deadmask >> k) & 1u)) continue;
-                if (rank < births) {
-                    const float ple = u01(r.v[k]);
-                    d.m_ple[4 * g + k] = ple;
-                    dd[k] = death_age(d.cdfm, d.am, ple);
-                    a[k] = 0;
-                    nsw &= ~(0xFFu << (8 * k));
-                    net[k] += 1;
-                    reborn = true;
-                }
-                rank += 1;
-            }
-        }
-        if (aged || reborn) reinterpret_cast<int4*>(d.m_age)[g] = make_int4(a[0], a[1], a[2], a[3]);
-        if (reborn) reinterpret_cast<int4*>(d.m_dage)[g] = make_int4(dd[0], dd[1], dd[2], dd[3]);
-        if (nsw != sw) reinterpret_cast<unsigned int*>(d.m_state)[g] = nsw;
-        // Alive count per community: one atomic per tile when the tile lies in one community.
-        const uint32_t tile_end = min((b + 1) * kTile, d.M);
-        const bool single = __ldg(&d.mloc[c0 + 1]) >= tile_end;
-        if (single) {
-            const int sum = __reduce_add_sync(kFull, (unsigned)(net[0] + net[1] + net[2] + net[3]));
-            if (lane == 0 && sum != 0) atomicAdd(&d.mcnt[c0], (unsigned)sum);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (net[k] != 0) atomicAdd(&d.mcnt[slot_comm(d, c0, 4 * g + k)], (unsigned)net[k]);
+            const int net = (int)((born >> k) & 1u) - (int)((dim >> k) & 1u);
+            if (net != 0) atomicAdd(&d.mcnt[slot_comm(d, c0, 4 * g + k)], (unsigned)net);
         }
     }
+    // Draw groups: lane gi computes the Philox call of reborn group gi of the quad.
+    for (uint32_t gi = lane; gi < gtot; gi += 32) {
+        uint32_t u = 0;
+#pragma unroll
+        for (uint32_t v = 1; v < kQuad; ++v)
+            if (gi >= ((gst >> (8 * v)) & 0xFFu) && ((nb_pack >> (8 * v)) & 0xFFu)) u = v;
+        const uint32_t r4 = gi - ((gst >> (8 * u)) & 0xFFu);
+        const U4 v4 = draw4(key, kMosquitoRebirth, b0 + u, t, r4);
+        sm.draw[u][r4] = make_uint4(v4.v[0], v4.v[1], v4.v[2], v4.v[3]);
+    }
+    __syncwarp();
+    // Rank lanes: reborn slot j of the quad (tile u, rank r).
+    const uint32_t rtot = (nb_pack & 0xFFu) + ((nb_pack >> 8) & 0xFFu) + ((nb_pack >> 16) & 0xFFu) + (nb_pack >> 24);
+    for (uint32_t j = lane; j < rtot; j += 32) {
+        uint32_t u = 0, base = 0;
+#pragma unroll
+        for (uint32_t v = 0; v + 1 < kQuad; ++v) {
+            const uint32_t nbv = (nb_pack >> (8 * v)) & 0xFFu;
+            if (u == v && j >= base + nbv) {
+                base += nbv;
+                u = v + 1;
+            }
+        }
+        const uint32_t r = j - base;
+        const uint32_t i = (b0 + u) * kTile + sm.slot[u][r];
+        const uint4 v4 = sm.draw[u][r >> 2];
+        const uint32_t c = r & 3u;
+        const float ple = u01(c == 0 ? v4.x : c == 1 ? v4.y : c == 2 ? v4.z : v4.w);
+        d.m_ple[i] = ple;
+        d.m_dage[i] = death_age_m(d.cdfm, d.minv, d.am, ple);
+        d.m_age[i] = 0;
+    }
+    __syncwarp();
 }
 
 template <int U>
-__global__ void __launch_bounds__(512) k_demog(Dev d, uint32_t hblocks)
+__global__ void __launch_bounds__(256) k_demog(Dev d, uint32_t hblocks, uint32_t koff)
 {
-    const uint32_t t = d.ctrl->t;
+    __shared__ QuadSmem wsm[8];
+    const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
     if (blockIdx.x < hblocks) {
         demog_humans<U>(d, key, blockIdx.x * blockDim.x * U + threadIdx.x, blockDim.x, t);
     } else {
         const uint32_t wpb = blockDim.x >> 5;
         const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-        demog_mosquitoes<U>(d, key, (blockIdx.x - hblocks) * wpb * U + warp, wpb, lane, t);
+        const uint32_t q = (blockIdx.x - hblocks) * wpb + warp;
+        if (q * kQuad < d.tiles) demog_mosquito_quad(d, key, q, lane, t, wsm[warp]);
     }
 }
 
 // ------------------------------------------------------------------ series + force of infection
 
-// Events of one source pair spread by the whole warp, four per Philox call per lane.
-__device__ __forceinline__ void spread_events(const Dev& d, const Key& key, uint32_t* trans, uint32_t stream_local, uint32_t stream_long,
-                                              uint32_t pidx, uint32_t s, uint32_t nlocal, uint32_t nlong, uint32_t loc,
-                                              uint32_t deg, uint32_t lane, uint32_t t)
-{
-    const uint32_t row = s * d.P;
-    for (uint32_t base = lane * 4; base < nlocal; base += 128) {
-        const U4 r = draw4(key, stream_local, pidx, t, base >> 2);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (base + q < nlocal) atomicAdd(&trans[row + __ldg(&d.csr_to[loc + bounded(r.v[q], deg)])], 1u);
-    }
-    for (uint32_t base = lane * 4; base < nlong; base += 128) {
-        const U4 r = draw4(key, stream_long, pidx, t, base >> 2);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (base + q < nlong) atomicAdd(&trans[row + bounded(r.v[q], d.P)], 1u);
-    }
-}
-
-// Event count of a source and its split (cpp/nepidemic.cu:65-136). Returns the local and
-// long-distance counts; the events that stay are added to trans[pidx] here.
-__device__ __forceinline__ void split_events(const Dev& d, uint32_t* trans, float x, const U4& r, uint32_t pidx, uint32_t c,
-                                             uint32_t* nlocal, uint32_t* nlong, uint32_t* loc, uint32_t* deg)
+// Event count of a source and its split (cpp/nepidemic.cu:65-136): a noDistance share stays
+// home (added to trans[pidx] here), a longDistance share of the rest goes to uniform
+// communities, the remainder to uniform CSR neighbours; an isolated community keeps all.
+__device__ __forceinline__ void split_events(const Dev& d, uint32_t* trans, float x, const U4& r, uint32_t pidx,
+                                             uint32_t deg, uint32_t* nlocal, uint32_t* nlong)
 {
     uint32_t n = (uint32_t)resolve(x, r.v[0]);
     if (n >= (1u << 26)) {
         atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
         n = (1u << 26) - 1;
     }
-    *loc = __ldg(&d.csr_loc[c]);
-    *deg = __ldg(&d.csr_loc[c + 1]) - *loc;
     uint32_t stay = n, lng = 0;
-    if (*deg > 0) {
+    if (deg > 0) {
         stay = (uint32_t)resolve(__fmul_rn((float)n, d.noDist), r.v[1]);
         n -= stay;
         lng = (uint32_t)resolve(__fmul_rn((float)n, d.longDist), r.v[2]);
@@ -368,84 +482,124 @@ __device__ __forceinline__ void split_events(const Dev& d, uint32_t* trans, floa
     *nlong = lng;
 }
 
-__global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only)
+// Series row + force of infection. A CTA of 4*K threads owns K consecutive (serotype,
+// community) pairs: K threads read the counters, add the series sums and split each pair's
+// events; then all threads spread the flattened events of the K pairs, four per Philox call.
+__global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t koff)
 {
-    const uint32_t t = d.ctrl->t;
+    __shared__ uint32_t s_cnt[512], s_scan[513], s_loc[128], s_deg[128], s_sum[3 * ARBO_MAX_STRAINS + 2],
+        s_wt[16];
+    const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
     const uint32_t row = collect_only ? 0u : t + 1;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t SP = d.S * d.P;
-    if (gw * 32 >= SP) return;  // warp-uniform
-    const uint32_t p = gw * 32 + lane;
-    const bool valid = p < SP;
-    const uint32_t s = valid ? p / d.P : 0u;
-    const uint32_t c = valid ? p - s * d.P : 0u;
-    const uint32_t ih = valid ? d.infh[p] : 0u;
-    const uint32_t im = valid ? d.infm[p] : 0u;
-    const uint32_t ic = valid ? d.inc[p] : 0u;
-    if (valid && ic) d.inc[p] = 0u;
-
-    // Series row (cpp/datacollect.cu:79-189): sums over communities per serotype.
-    const uint32_t s_lo = __shfl_sync(kFull, s, 0);
-    const uint32_t s_hi = __reduce_max_sync(kFull, s);
-    for (uint32_t ss = s_lo; ss <= s_hi; ++ss) {
-        const bool mine = valid && s == ss;
-        const uint32_t a = __reduce_add_sync(kFull, mine ? ih : 0u);
-        const uint32_t b = __reduce_add_sync(kFull, mine ? ic : 0u);
-        const uint32_t m = __reduce_add_sync(kFull, mine ? im : 0u);
-        if (lane == 0) {
-            if (a) atomicAdd(&d.s_ninf[row * d.S + ss], a);
-            if (b) atomicAdd(&d.s_ninc[row * d.S + ss], b);
-            if (m) atomicAdd(&d.s_minf[row * d.S + ss], m);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t K = blockDim.x >> 2;
+    const uint32_t SP = d.S * d.P, S = d.S, P = d.P;
+    const uint32_t p0 = blockIdx.x * K;
+    if (tid < 3 * ARBO_MAX_STRAINS + 2) s_sum[tid] = 0;
+    __syncthreads();
+    uint32_t nk[4] = {0, 0, 0, 0};
+    if (tid < K) {
+        const uint32_t p = p0 + tid;
+        if (p < SP) {
+            // Every independent load and draw first, then the arithmetic.
+            const uint32_t s = p / P, c = p - s * P;
+            const uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
+            const uint32_t ncc = __ldg(&d.ncnt[c]), mcc = d.mcnt[c];
+            const uint32_t loc = __ldg(&d.csr_loc[c]), loc1 = __ldg(&d.csr_loc[c + 1]);
+            U4 rh, rm;
+            if (!collect_only) {
+                rh = draw4(key, kFoiHM, p, t);
+                rm = draw4(key, kFoiMH, p, t);
+            }
+            if (ic) d.inc[p] = 0u;
+            if (ih) atomicAdd(&s_sum[s], ih);
+            if (ic) atomicAdd(&s_sum[ARBO_MAX_STRAINS + s], ic);
+            if (im) atomicAdd(&s_sum[2 * ARBO_MAX_STRAINS + s], im);
+            if (c == 0) d.s_one[row * S + s] = ih;
+            if (s == 0) {
+                atomicAdd(&s_sum[3 * ARBO_MAX_STRAINS], ncc);
+                atomicAdd(&s_sum[3 * ARBO_MAX_STRAINS + 1], mcc);
+            }
+            if (d.recordSpatial) d.s_spatial[(size_t)row * SP + p] = ih;
+            if (!collect_only && (ih | im)) {
+                const uint32_t deg = loc1 - loc;
+                s_loc[tid] = loc;
+                s_deg[tid] = deg;
+                if (ih > 0) {  // human -> mosquito (cpp/nepidemic.cu:28-142)
+                    const float ratio = __fdiv_rn((float)mcc, (float)ncc);
+                    float x = __fmul_rn(ratio, d.biting);
+                    x = __fmul_rn(x, d.nmSuccess);
+                    x = __fmul_rn(x, (float)ih);
+                    split_events(d, d.transm, x, rh, p, deg, &nk[0], &nk[1]);
+                }
+                if (im > 0) {  // mosquito -> human (cpp/mepidemic.cu:28-138)
+                    float x = __fmul_rn(d.biting, d.mnSuccess);
+                    x = __fmul_rn(x, (float)im);
+                    split_events(d, d.transh, x, rm, p, deg, &nk[2], &nk[3]);
+                }
+            }
         }
     }
-    if (valid && c == 0) d.s_one[row * d.S + s] = ih;
-    const bool first = valid && s == 0;
-    const uint32_t nc = __reduce_add_sync(kFull, first ? __ldg(&d.ncnt[c]) : 0u);
-    const uint32_t mc_sum = __reduce_add_sync(kFull, first ? d.mcnt[c] : 0u);
-    if (lane == 0) {
-        if (nc) atomicAdd(&d.s_ncount[row], nc);
-        if (mc_sum) atomicAdd(&d.s_mcount[row], mc_sum);
+    // s_cnt[4*pair + kind] for kind 0 HM local, 1 HM long, 2 MH local, 3 MH long
+    if (tid < K) {
+#pragma unroll
+        for (int kd = 0; kd < 4; ++kd) s_cnt[4 * tid + kd] = nk[kd];
     }
-    if (d.recordSpatial && valid) d.s_spatial[(size_t)row * SP + p] = ih;
+    __syncthreads();
+    if (tid < 3 * S) {
+        const uint32_t kind = tid / S, s = tid - kind * S;
+        const uint32_t v = s_sum[kind * ARBO_MAX_STRAINS + s];
+        uint32_t* dst = kind == 0 ? d.s_ninf : kind == 1 ? d.s_ninc : d.s_minf;
+        if (v) atomicAdd(&dst[row * S + s], v);
+    } else if (tid == 3 * S) {
+        if (s_sum[3 * ARBO_MAX_STRAINS]) atomicAdd(&d.s_ncount[row], s_sum[3 * ARBO_MAX_STRAINS]);
+        if (s_sum[3 * ARBO_MAX_STRAINS + 1]) atomicAdd(&d.s_mcount[row], s_sum[3 * ARBO_MAX_STRAINS + 1]);
+    }
     if (collect_only) return;
-
-    // Force of infection: human -> mosquito (cpp/nepidemic.cu:28-142).
-    uint32_t hl = 0, hg = 0, hloc = 0, hdeg = 0;
-    if (ih > 0) {
-        const U4 r = draw4(key, kFoiHM, p, t);
-        const float ratio = __fdiv_rn((float)d.mcnt[c], (float)__ldg(&d.ncnt[c]));
-        float x = __fmul_rn(ratio, d.biting);
-        x = __fmul_rn(x, d.nmSuccess);
-        x = __fmul_rn(x, (float)ih);
-        split_events(d, d.transm, x, r, p, c, &hl, &hg, &hloc, &hdeg);
+    // Exclusive scan of the groups of four events of every (pair, kind) entry.
+    uint32_t v = (s_cnt[tid] + 3) >> 2;
+    const uint32_t own = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, v, off);
+        if (lane >= (uint32_t)off) v += y;
     }
-    // Mosquito -> human (cpp/mepidemic.cu:28-138).
-    uint32_t ml = 0, mg = 0, mloc = 0, mdeg = 0;
-    if (im > 0) {
-        const U4 r = draw4(key, kFoiMH, p, t);
-        float x = __fmul_rn(d.biting, d.mnSuccess);
-        x = __fmul_rn(x, (float)im);
-        split_events(d, d.transh, x, r, p, c, &ml, &mg, &mloc, &mdeg);
+    if (lane == 31) s_wt[warp] = v;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+            const uint32_t x = s_wt[w];
+            s_wt[w] = acc;
+            acc += x;
+        }
+        s_scan[blockDim.x] = acc;
     }
-    unsigned act = __ballot_sync(kFull, (hl | hg) != 0u);
-    while (act) {
-        const uint32_t src = __ffs(act) - 1;
-        act &= act - 1;
-        const uint32_t sp = __shfl_sync(kFull, p, src), ss = __shfl_sync(kFull, s, src);
-        const uint32_t nl = __shfl_sync(kFull, hl, src), ng = __shfl_sync(kFull, hg, src);
-        const uint32_t lo = __shfl_sync(kFull, hloc, src), dg = __shfl_sync(kFull, hdeg, src);
-        spread_events(d, key, d.transm, kFoiHMLocal, kFoiHMLong, sp, ss, nl, ng, lo, dg, lane, t);
-    }
-    act = __ballot_sync(kFull, (ml | mg) != 0u);
-    while (act) {
-        const uint32_t src = __ffs(act) - 1;
-        act &= act - 1;
-        const uint32_t sp = __shfl_sync(kFull, p, src), ss = __shfl_sync(kFull, s, src);
-        const uint32_t nl = __shfl_sync(kFull, ml, src), ng = __shfl_sync(kFull, mg, src);
-        const uint32_t lo = __shfl_sync(kFull, mloc, src), dg = __shfl_sync(kFull, mdeg, src);
-        spread_events(d, key, d.transh, kFoiMHLocal, kFoiMHLong, sp, ss, nl, ng, lo, dg, lane, t);
+    __syncthreads();
+    s_scan[tid] = v - own + s_wt[warp];
+    __syncthreads();
+    const uint32_t G = s_scan[blockDim.x];
+    for (uint32_t gi = tid; gi < G; gi += blockDim.x) {
+        uint32_t lo = 0, hi = blockDim.x - 1;  // last entry with s_scan[entry] <= gi
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (s_scan[mid] <= gi) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t entry = lo, pair = entry >> 2, kind = entry & 3u;
+        const uint32_t r4 = gi - s_scan[entry];
+        const uint32_t p = p0 + pair, s = p / P;
+        const uint32_t n = s_cnt[entry];
+        const uint32_t stream = kind == 0 ? kFoiHMLocal : kind == 1 ? kFoiHMLong : kind == 2 ? kFoiMHLocal : kFoiMHLong;
+        uint32_t* trans = kind < 2 ? d.transm : d.transh;
+        const U4 r = draw4(key, stream, p, t, r4);
+        const uint32_t loc = s_loc[pair], deg = s_deg[pair];
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) {
+            if (4 * r4 + qq >= n) break;
+            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : __ldg(&d.csr_to[loc + bounded(r.v[qq], deg)]);
+            atomicAdd(&trans[s * P + dest], 1u);
+        }
     }
 }
 
@@ -463,8 +617,8 @@ __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t 
 
 // Target of mosquito event e: the first alive slot of its attempt sequence (dead slots are
 // retried, cpp/mepidemic.cu:206-235). Returns UINT_MAX when the attempts run out.
-__device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key, uint32_t pidx, uint32_t e, uint32_t base,
-                                                    uint32_t size, uint32_t t)
+__device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key, uint32_t pidx, uint32_t e,
+                                                    uint32_t base, uint32_t size, uint32_t t)
 {
     for (uint32_t a = 0; a < d.maxTarget; a += 4) {
         const U4 r = draw4(key, kInfMTarget, pidx, t, e, a >> 2);
@@ -478,156 +632,229 @@ __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key
     return UINT_MAX;
 }
 
-__global__ void __launch_bounds__(512) k_infect(Dev d)
-{
-    __shared__ uint32_t sh_kh[ARBO_MAX_STRAINS], sh_km[ARBO_MAX_STRAINS], sh_ne[ARBO_MAX_STRAINS];
-    __shared__ uint32_t sh_s0h, sh_s0m, sh_any;
-    const uint32_t t = d.ctrl->t;
-    const uint32_t epoch = d.ctrl->epoch;
-    const Key key = load_key(d.ctrl);
-    const uint32_t hiword = ~epoch;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t S = d.S, P = d.P;
+// Per-CTA tables of the infection kernel: the CTA's K communities (one per warp) and their
+// events of every serotype flattened into one index space.
+struct InfectSmem {
+    uint32_t cstart[17];                 // flattened item start of each community (K+1)
+    uint32_t hstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, human groups
+    uint32_t mstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, mosquito events
+    uint32_t kh[16][ARBO_MAX_STRAINS];     // human events by position
+    uint32_t km[16][ARBO_MAX_STRAINS];     // mosquito events by position
+    uint32_t hitems[16];                 // human groups of the community
+    uint32_t c[16], s0h[16], s0m[16], nbase[16], mbase[16], ns[16], ms[16];
+};
 
-    for (uint32_t c = blockIdx.x; c < P; c += gridDim.x) {
-        const uint32_t ns = __ldg(&d.nsize[c]);
-        const uint32_t ms = __ldg(&d.msize[c]);
-        const uint32_t mc = d.mcnt[c];
-        if (tid == 0) {
-            sh_s0m = mc ? bounded(draw4(key, kInfMStart, c, t).v[0], S) : 0u;
-            sh_s0h = ns ? bounded(draw4(key, kInfHStart, c, t).v[0], S) : 0u;
-            sh_any = 0;
-        }
-        __syncthreads();
-        if (tid < S) {
-            const uint32_t sh = (sh_s0h + tid) % S, ph = sh * P + c;
-            uint32_t kh = d.transh[ph];
-            if (kh) d.transh[ph] = 0;
-            uint32_t ne = 0;
-            if (ns == 0) kh = 0;
-            else ne = (uint32_t)resolve(__fdiv_rn(d.extInf, (float)P), draw4(key, kIntroCount, ph, t).v[0]);
-            const uint32_t sm = (sh_s0m + tid) % S, pm = sm * P + c;
-            uint32_t km = d.transm[pm];
-            if (km) d.transm[pm] = 0;
-            if (mc == 0) km = 0;
-            if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
-                atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
-                kh = min(kh, kMaxEventsPerPair - 1);
-                km = min(km, kMaxEventsPerPair - 1);
-            }
-            sh_kh[tid] = kh;
-            sh_km[tid] = km;
-            sh_ne[tid] = ne;
-            if (kh | km | ne) atomicOr(&sh_any, 1u);
-        }
-        __syncthreads();
-        if (sh_any) {
-            const uint32_t s0h = sh_s0h, s0m = sh_s0m;
-            const uint32_t nbase = __ldg(&d.nloc[c]), mbase = __ldg(&d.mloc[c]);
-            // Phase A: every event whose target is eligible at the start of the pass bids its
-            // serial order (serotype position j, then event index) for the target.
-            for (uint32_t j = 0; j < S; ++j) {
-                const uint32_t s = (s0h + j) % S, ph = s * P + c, k = sh_kh[j];
-                for (uint32_t base = 4 * tid; base < k; base += 4 * blockDim.x) {
-                    const U4 r = draw4(key, kInfHTarget, ph, t, base >> 2);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t e = base + q;
-                        if (e >= k) break;
-                        const uint32_t i = nbase + bounded(r.v[q], ns);
-                        if (d.n_status[i] == 0 && !((d.n_imm[i] >> s) & 1u))
-                            atomicMin(&d.winh[i], order_key(hiword, j, 0, e));
-                    }
+// Decodes flattened item `it` of the CTA: community slot w, serotype position j, and either a
+// human group r4 (human == true) or a mosquito event e.
+__device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, uint32_t S, uint32_t it, uint32_t* w,
+                                            uint32_t* j, bool* human, uint32_t* idx)
+{
+    uint32_t ww = 0;
+    while (ww + 1 < K && sh.cstart[ww + 1] <= it) ++ww;
+    uint32_t rel = it - sh.cstart[ww];
+    *w = ww;
+    if (rel < sh.hitems[ww]) {
+        uint32_t jj = 0;
+        while (jj + 1 < S && sh.hstart[ww][jj + 1] <= rel) ++jj;
+        *j = jj;
+        *human = true;
+        *idx = rel - sh.hstart[ww][jj];
+    } else {
+        rel -= sh.hitems[ww];
+        uint32_t jj = 0;
+        while (jj + 1 < S && sh.mstart[ww][jj + 1] <= rel) ++jj;
+        *j = jj;
+        *human = false;
+        *idx = rel - sh.mstart[ww][jj];
+    }
+}
+
+// Infection draws. A CTA of K warps owns K communities. Warp w reads its community's event
+// counts (lanes 0..S-1), draws its introduction counts and first serotypes in parallel lanes, and
+// posts the per-serotype tables; the events of the K communities (groups of four human events,
+// single mosquito events) then form one index space shared by all the CTA's threads:
+//   A: every event whose target is eligible at the start of the pass bids its serial order
+//      (serotype position j, event index) for the target with atomicMin;
+//   B: external introductions (cpp/nepidemic.cu:261-309), per community in serial order, one warp
+//      testing 32 attempts at a time;
+//   C: each event that won its target applies its infection.
+// This reproduces the serial loops of nmTransmission / mnTransmission (cpp/mepidemic.cu:143-246,
+// cpp/nepidemic.cu:146-319): a target is infected by the first eligible event in serial order.
+__global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
+{
+    __shared__ InfectSmem sh;
+    const uint32_t t = d.ctrl->t + koff;
+    const uint32_t epoch = d.ctrl->epoch + koff;
+    const uint32_t hiword = ~epoch;
+    const Key key = load_key(d.ctrl);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t K = blockDim.x >> 5;
+    const uint32_t S = d.S, P = d.P;
+    const float ext = __fdiv_rn(d.extInf, (float)P);
+
+    for (uint32_t cb = blockIdx.x * K; cb < P; cb += gridDim.x * K) {
+        const uint32_t c = cb + warp;
+        uint32_t ne = 0;
+        uint32_t items = 0;
+        if (c < P) {
+            // Loads that do not depend on the step first, then the keyed draws.
+            const uint32_t ns = __ldg(&d.nsize[c]);
+            const uint32_t ms = __ldg(&d.msize[c]);
+            const uint32_t nb0 = __ldg(&d.nloc[c]), mb0 = __ldg(&d.mloc[c]);
+            const uint32_t mc = d.mcnt[c];
+            const uint32_t pl = lane * P + c;
+            uint32_t kh = lane < S ? d.transh[pl] : 0u;
+            uint32_t km = lane < S ? d.transm[pl] : 0u;
+            uint32_t sv = 0;
+            if (lane < S) {
+                const U4 rn = draw4(key, kIntroCount, pl, t);
+                if (kh) d.transh[pl] = 0;
+                if (km) d.transm[pl] = 0;
+                if (ns == 0) kh = 0;
+                else ne = (uint32_t)resolve(ext, rn.v[0]);
+                if (mc == 0) km = 0;
+                if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
+                    atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
+                    kh = min(kh, kMaxEventsPerPair - 1);
+                    km = min(km, kMaxEventsPerPair - 1);
                 }
-                const uint32_t sm = (s0m + j) % S, pm = sm * P + c, km = sh_km[j];
-                for (uint32_t e = tid; e < km; e += blockDim.x) {
-                    const uint32_t slot = mosquito_target(d, key, pm, e, mbase, ms, t);
-                    if (slot == UINT_MAX) {
-                        atomicAdd(&d.ctrl->diag[0], 1u);
+            } else if (lane == 8) {
+                const U4 r = draw4(key, kInfMStart, c, t);
+                if (mc) sv = bounded(r.v[0], S);
+            } else if (lane == 9) {
+                const U4 r = draw4(key, kInfHStart, c, t);
+                if (ns) sv = bounded(r.v[0], S);
+            }
+            const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
+            uint32_t H = 0, Mt = 0;
+            for (uint32_t j = 0; j < S; ++j) {
+                const uint32_t khj = __shfl_sync(kFull, kh, (s0h + j) % S);
+                const uint32_t kmj = __shfl_sync(kFull, km, (s0m + j) % S);
+                if (lane == 0) {
+                    sh.hstart[warp][j] = H;
+                    sh.mstart[warp][j] = Mt;
+                    sh.kh[warp][j] = khj;
+                    sh.km[warp][j] = kmj;
+                }
+                H += (khj + 3) >> 2;
+                Mt += kmj;
+            }
+            if (lane == 0) {
+                sh.hitems[warp] = H;
+                sh.c[warp] = c;
+                sh.s0h[warp] = s0h;
+                sh.s0m[warp] = s0m;
+                sh.nbase[warp] = nb0;
+                sh.mbase[warp] = mb0;
+                sh.ns[warp] = ns;
+                sh.ms[warp] = ms;
+            }
+            items = H + Mt;
+        }
+        // Item starts of the K communities (warp totals, serial over at most 16 warps).
+        if (lane == 0) sh.cstart[warp + 1] = items;
+        __syncthreads();
+        if (tid == 0) {
+            sh.cstart[0] = 0;
+            for (uint32_t w = 1; w <= K; ++w) sh.cstart[w] += sh.cstart[w - 1];
+        }
+        __syncthreads();
+        const uint32_t total = sh.cstart[K];
+        const uint32_t any_intro = __syncthreads_or(ne != 0);
+        if (total == 0 && !any_intro) continue;
+
+        // Phase A
+        for (uint32_t it = tid; it < total; it += blockDim.x) {
+            uint32_t w, j, idx;
+            bool human;
+            decode_item(sh, K, S, it, &w, &j, &human, &idx);
+            const uint32_t cc = sh.c[w];
+            if (human) {
+                const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+                const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t e = 4 * idx + q;
+                    if (e >= k) break;
+                    const uint32_t i = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+                    const uint32_t st = d.n_status[i], im = d.n_imm[i];
+                    if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[i], order_key(hiword, j, 0, e));
+                }
+            } else {
+                const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+                const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+                if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
+                else if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
+            }
+        }
+        __syncthreads();
+        // Phase B: warp w handles the introductions of its own community.
+        if (any_intro && c < P) {
+            const uint32_t s0h = sh.s0h[warp], nbase = sh.nbase[warp], ns = sh.ns[warp];
+            for (uint32_t j = 0; j < S; ++j) {
+                const uint32_t s = (s0h + j) % S, ph = s * P + c;
+                uint32_t left = __shfl_sync(kFull, ne, s);
+                if (left == 0) continue;
+                uint32_t a0 = 0;
+                while (left > 0 && a0 < d.maxIntro) {
+                    const uint32_t a = a0 + lane;
+                    bool elig = false;
+                    uint32_t i = 0;
+                    unsigned long long okey = 0;
+                    if (a < d.maxIntro) {
+                        const U4 r = draw4(key, kIntroTarget, ph, t, a >> 2);
+                        i = nbase + bounded(r.v[a & 3], ns);
+                        okey = order_key(hiword, j, 1, a);
+                        elig = __ldcg(&d.n_status[i]) == 0 && !((__ldcg(&d.n_imm[i]) >> s) & 1u) &&
+                               __ldcg(&d.winh[i]) > okey;
+                    }
+                    const unsigned bal = __ballot_sync(kFull, elig);
+                    if (!bal) {
+                        a0 += 32;
                         continue;
                     }
-                    if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, e));
-                }
-            }
-            __syncthreads();
-            // Phase B: external introductions (cpp/nepidemic.cu:261-309), in serial order, one
-            // warp testing 32 attempts at a time; an attempt succeeds on a target that is
-            // susceptible, naive to the serotype and not won by an earlier event.
-            if (warp == 0) {
-                for (uint32_t j = 0; j < S; ++j) {
-                    uint32_t ne = sh_ne[j];
-                    if (ne == 0) continue;
-                    const uint32_t s = (s0h + j) % S, ph = s * P + c;
-                    uint32_t a0 = 0;
-                    while (ne > 0 && a0 < d.maxIntro) {
-                        const uint32_t a = a0 + lane;
-                        bool elig = false;
-                        uint32_t i = 0;
-                        unsigned long long okey = 0;
-                        if (a < d.maxIntro) {
-                            const U4 r = draw4(key, kIntroTarget, ph, t, a >> 2);
-                            i = nbase + bounded(r.v[a & 3], ns);
-                            okey = order_key(hiword, j, 1, a);
-                            elig = __ldcg(&d.n_status[i]) == 0 && !((__ldcg(&d.n_imm[i]) >> s) & 1u) &&
-                                   __ldcg(&d.winh[i]) > okey;
-                        }
-                        const unsigned bal = __ballot_sync(kFull, elig);
-                        if (!bal) {
-                            a0 += 32;
-                            continue;
-                        }
-                        const uint32_t pl = __ffs(bal) - 1;
-                        if (lane == pl) {
-                            d.winh[i] = okey;
-                            infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a));
-                        }
-                        __syncwarp();
-                        ne -= 1;
-                        a0 = a0 + pl + 1;
+                    const uint32_t pl = __ffs(bal) - 1;
+                    if (lane == pl) {
+                        d.winh[i] = okey;
+                        infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a));
                     }
-                    if (ne > 0 && lane == 0) atomicAdd(&d.ctrl->diag[1], 1u);
+                    __syncwarp();
+                    left -= 1;
+                    a0 = a0 + pl + 1;
                 }
+                if (left > 0 && lane == 0) atomicAdd(&d.ctrl->diag[1], 1u);
             }
-            __syncthreads();
-            // Phase C: each event that won its target applies its infection.
-            for (uint32_t j = 0; j < S; ++j) {
-                const uint32_t s = (s0h + j) % S, ph = s * P + c, k = sh_kh[j];
-                for (uint32_t base = 4 * tid; base < k; base += 4 * blockDim.x) {
-                    const U4 r = draw4(key, kInfHTarget, ph, t, base >> 2);
+        }
+        __syncthreads();
+        // Phase C
+        for (uint32_t it = tid; it < total; it += blockDim.x) {
+            uint32_t w, j, idx;
+            bool human;
+            decode_item(sh, K, S, it, &w, &j, &human, &idx);
+            const uint32_t cc = sh.c[w];
+            if (human) {
+                const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+                const U4 r = draw4(key, kInfHTarget, ph, t, idx);
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t e = base + q;
-                        if (e >= k) break;
-                        const uint32_t i = nbase + bounded(r.v[q], ns);
-                        if (__ldcg(&d.winh[i]) == order_key(hiword, j, 0, e))
-                            infect_human(d, i, s, draw4(key, kInfHExposed, ph, t, e));
-                    }
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t e = 4 * idx + q;
+                    if (e >= k) break;
+                    const uint32_t i = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+                    if (__ldcg(&d.winh[i]) == order_key(hiword, j, 0, e))
+                        infect_human(d, i, s, draw4(key, kInfHExposed, ph, t, e));
                 }
-                const uint32_t sm = (s0m + j) % S, pm = sm * P + c, km = sh_km[j];
-                for (uint32_t e = tid; e < km; e += blockDim.x) {
-                    const uint32_t slot = mosquito_target(d, key, pm, e, mbase, ms, t);
-                    if (slot == UINT_MAX) continue;
-                    if (__ldcg(&d.winm[slot]) == order_key(hiword, j, 0, e)) {
-                        const U4 r = draw4(key, kInfMExposed, pm, t, e >> 2);
-                        d.m_state[slot] = 1;
-                        d.m_strain[slot] = (uint8_t)sm;
-                        d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)d.m_age[slot], d.mExposed), r.v[e & 3]);
-                    }
+            } else {
+                const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+                const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+                if (slot != UINT_MAX && __ldcg(&d.winm[slot]) == order_key(hiword, j, 0, idx)) {
+                    const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
+                    d.m_state[slot] = 1;
+                    d.m_strain[slot] = (uint8_t)sm;
+                    d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)d.m_age[slot], d.mExposed), r.v[idx & 3]);
                 }
             }
         }
         __syncthreads();
-    }
-    // The last CTA to finish advances the step counter and the winner epoch.
-    if (tid == 0) {
-        __threadfence();
-        const uint32_t prev = atomicAdd(&d.ctrl->done, 1u);
-        if (prev == gridDim.x - 1) {
-            d.ctrl->done = 0;
-            d.ctrl->t = t + 1;
-            d.ctrl->epoch = epoch + 1;
-            __threadfence();
-        }
     }
 }
 
@@ -713,7 +940,7 @@ __global__ void k_init_mosquitoes(Dev d)
             d.m_state[i] = 0;
             d.m_age[i] = (int32_t)a;
             d.m_ple[i] = ple;
-            d.m_dage[i] = death_age(d.cdfm, d.am, ple);
+            d.m_dage[i] = death_age_m(d.cdfm, d.minv, d.am, ple);
         }
     }
     const uint32_t tile_dead = __reduce_add_sync(kFull, ndead);
@@ -772,6 +999,16 @@ __global__ void __launch_bounds__(256) k_l2_flush(const int4* __restrict__ buf, 
     if (acc == 0x9E3779B9u) *sink = acc;
 }
 
+// Advances the step counter and the winner epoch after `n` captured steps (steps inside a
+// graph read ctrl->t plus their baked offset).
+__global__ void k_advance(Dev d, uint32_t n)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        d.ctrl->t += n;
+        d.ctrl->epoch += n;
+    }
+}
+
 }  // namespace
 
 int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_sm, cudaStream_t st)
@@ -780,32 +1017,44 @@ int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_
     return (int)cudaGetLastError();
 }
 
-int launch_demog(const Dev& d, const Launch& l, cudaStream_t st)
+int demog_blocks_per_sm(uint32_t unroll, uint32_t block)
+{
+    int n = 0;
+    cudaError_t e;
+    if (unroll == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog<4>, (int)block, 0);
+    else if (unroll == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog<2>, (int)block, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog<1>, (int)block, 0);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
+int launch_demog(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 {
     const uint32_t U = l.demogUnroll;
     const uint32_t hblocks = cdiv(d.nvec, (uint64_t)l.demogBlock * U);
-    const uint32_t mblocks = cdiv(d.tiles, (uint64_t)(l.demogBlock / 32) * U);
+    const uint32_t quads = cdiv(d.tiles, kQuad);
+    const uint32_t mblocks = cdiv(quads, l.demogBlock / 32);
     const dim3 grid(hblocks + mblocks), block(l.demogBlock);
-    if (U == 4) k_demog<4><<<grid, block, 0, st>>>(d, hblocks);
-    else if (U == 2) k_demog<2><<<grid, block, 0, st>>>(d, hblocks);
-    else k_demog<1><<<grid, block, 0, st>>>(d, hblocks);
+    if (U == 4) k_demog<4><<<grid, block, 0, st>>>(d, hblocks, koff);
+    else if (U == 2) k_demog<2><<<grid, block, 0, st>>>(d, hblocks, koff);
+    else k_demog<1><<<grid, block, 0, st>>>(d, hblocks, koff);
     return (int)cudaGetLastError();
 }
 
-int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only)
+int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only, uint32_t koff)
 {
     const uint32_t SP = d.S * d.P;
-    const uint32_t blocks = cdiv((uint64_t)cdiv(SP, 32) * 32, l.foiBlock);
-    k_foi<<<blocks, l.foiBlock, 0, st>>>(d, collect_only);
+    const uint32_t K = l.foiBlock / 4;
+    k_foi<<<cdiv(SP, K), l.foiBlock, 0, st>>>(d, collect_only, koff);
     return (int)cudaGetLastError();
 }
 
-int launch_infect(const Dev& d, const Launch& l, cudaStream_t st)
+int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 {
-    uint32_t blocks = d.P;
-    const uint32_t cap = 64u * (l.numSM ? l.numSM : 152u);
+    const uint32_t wpb = l.infectBlock / 32;
+    uint32_t blocks = cdiv(d.P, wpb);
+    const uint32_t cap = 16u * (l.numSM ? l.numSM : 152u);
     if (blocks > cap) blocks = cap;
-    k_infect<<<blocks, l.infectBlock, 0, st>>>(d);
+    k_infect<<<blocks, l.infectBlock, 0, st>>>(d, koff);
     return (int)cudaGetLastError();
 }
 
@@ -818,22 +1067,28 @@ int launch_init(const Dev& d, const Launch& l, void* stream)
     k_seed<<<cdiv(nseed ? nseed : 1, 256), 256, 0, st>>>(d);
     int e = (int)cudaGetLastError();
     if (e) return e;
-    return launch_foi(d, l, st, 1);
+    return launch_foi(d, l, st, 1, 0);
 }
 
-int launch_step(const Dev& d, const Launch& l, void* stream, void* events)
+int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint32_t koff)
 {
     cudaStream_t st = (cudaStream_t)stream;
     cudaEvent_t* ev = (cudaEvent_t*)events;
     int e;
     if (ev) cudaEventRecord(ev[0], st);
-    if ((e = launch_demog(d, l, st))) return e;
+    if ((e = launch_demog(d, l, st, koff))) return e;
     if (ev) cudaEventRecord(ev[1], st);
-    if ((e = launch_foi(d, l, st, 0))) return e;
+    if ((e = launch_foi(d, l, st, 0, koff))) return e;
     if (ev) cudaEventRecord(ev[2], st);
-    if ((e = launch_infect(d, l, st))) return e;
+    if ((e = launch_infect(d, l, st, koff))) return e;
     if (ev) cudaEventRecord(ev[3], st);
     return 0;
+}
+
+int launch_advance(const Dev& d, uint32_t n, void* stream)
+{
+    k_advance<<<1, 32, 0, (cudaStream_t)stream>>>(d, n);
+    return (int)cudaGetLastError();
 }
 
 uint32_t launches_per_step() { return 3; }

@@ -31,7 +31,7 @@ struct Ctrl {
     uint32_t t;          // current step
     uint32_t epoch;      // steps taken since the handle was created (winner tags)
     uint32_t err;        // ARBO_DEVERR_* bits
-    uint32_t done;       // CTAs finished in the infection kernel of this step
+    uint32_t done;       // unused (kept for layout)
     uint32_t diag[4];    // dropped mosquito events, exhausted introductions, -, -
     uint32_t k0, k1;     // random key (seed low / high word)
     uint32_t instance;   // 16-bit stream id of this simulation
@@ -81,6 +81,7 @@ struct Dev {
     // tables
     float* cdfh;
     float* cdfm;
+    uint32_t* minv;   // [4098] first mosquito age with CDF >= k/4096 (table size if none)
     float* survh;
     float* survm;
     float* etab;
@@ -99,13 +100,18 @@ struct Dev {
 };
 
 struct Launch {
-    uint32_t demogBlock, demogUnroll, foiBlock, infectBlock, numSM;
+    uint32_t demogBlock, demogUnroll, foiBlock, infectBlock, numSM, demogBlocksPerSM;
 };
 
 // Kernel launchers (kernels.cu). Each returns the cudaError_t of the launch as int.
 int launch_init(const Dev& d, const Launch& l, void* stream);
-// One time step; with events != null, records cudaEvent_t events[0..3] around the three kernels.
-int launch_step(const Dev& d, const Launch& l, void* stream, void* events);
+// Resident CTAs per SM of the demographic kernel for the given unroll and block size.
+int demog_blocks_per_sm(uint32_t unroll, uint32_t block);
+// One time step at offset koff from ctrl->t (the step counter advances only through
+// launch_advance); with events != null, records cudaEvent_t events[0..3] around the three kernels.
+int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint32_t koff);
+// Adds n to the step counter and the winner epoch (one thread).
+int launch_advance(const Dev& d, uint32_t n, void* stream);
 uint32_t launches_per_step();
 // Reads `bytes` of buf (a multiple of 16) to evict L2; `sink` is a device word never written in practice.
 int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_sm, cudaStream_t st);

@@ -474,11 +474,15 @@ static void demog_humans(oracle_sim* o, uint32_t t)
 }
 
 /* mBlockBirthDeath (cpp/mdemographic.cu:22-150) on logical 128-slot tiles: deaths, the
- * tile's stochastic birth quota from the carried dead count, rebirth of the lowest-index
- * dead slots, then the net change of each community's alive count. */
+ * tile's stochastic birth quota from the carried dead count, rebirth of dead slots in a fixed
+ * order, then the net change of each community's alive count. The reference reborns whichever
+ * dead slots win a shared-memory ticket race (cpp/mdemographic.cu:135); here the lowest-index
+ * dead slots of the tile are reborn first. Draws: the quota of tile b is component b&3 of the
+ * call keyed (b>>2, t); the r-th reborn slot of tile b takes component r&3 of the call keyed
+ * (b, t, r>>2). */
 static void demog_mosquitoes(oracle_sim* o, uint32_t t)
 {
-    uint32_t P = o->P, M = o->M;
+    uint32_t M = o->M, P = o->P;
     float E = o->etab[t + 1];
     uint32_t r[4];
     int32_t net[ARBO_MOSQUITO_TILE];
@@ -509,19 +513,19 @@ static void demog_mosquitoes(oracle_sim* o, uint32_t t)
         x = x / (float)M;
         x = x - fbt;
         x = x + (float)L;
-        draw(o, ST_M_TILE, b, t, 0, 0, r);
-        int32_t births = (int32_t)resolve(x, r[0]);
+        draw(o, ST_M_TILE, b >> 2, t, 0, 0, r);
+        int32_t births = (int32_t)resolve(x, r[b & 3]);
         o->ledger[b] = (int32_t)L - births;
         int32_t rank = 0;
         for (uint32_t k = 0; k < bt; ++k) {
             uint32_t i = i0 + k;
             if (!o->m_dead[i]) continue;
             if (rank < births) {
-                draw(o, ST_M_REBIRTH, i >> 2, t, 0, 0, r);
+                draw(o, ST_M_REBIRTH, b, t, (uint32_t)rank >> 2, 0, r);
                 o->m_age[i] = 0;
                 o->m_dead[i] = 0;
                 o->m_status[i] = 0;
-                o->m_ple[i] = u01(r[i & 3]);
+                o->m_ple[i] = u01(r[rank & 3]);
                 o->m_dage[i] = death_age(o->cdfm, o->am, o->m_ple[i]);
                 net[k] += 1;
             }

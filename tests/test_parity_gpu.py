@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 SHAPES = [
     dict(demogBlock=256, demogUnroll=2, foiBlock=256, infectBlock=256, graphSteps=64),
     dict(demogBlock=32, demogUnroll=1, foiBlock=32, infectBlock=32, graphSteps=0),
-    dict(demogBlock=512, demogUnroll=4, foiBlock=512, infectBlock=64, graphSteps=7),
+    dict(demogBlock=128, demogUnroll=4, foiBlock=512, infectBlock=64, graphSteps=7),
 ]
 
 
