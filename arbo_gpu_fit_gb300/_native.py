@@ -98,6 +98,7 @@ SIGNATURES = {
     "arbo_sim_launches_per_step": (c_uint32, [c_void_p]),
     "arbo_sim_write_incidence": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
+    "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
     "arbo_selftest_philox": (c_int, [POINTER(c_uint32), c_uint32, POINTER(c_uint32)]),
     "arbo_selftest_curand_philox": (c_int, [c_uint64, c_uint32, POINTER(c_uint32)]),
 }

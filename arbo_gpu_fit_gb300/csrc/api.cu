@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -990,3 +991,63 @@ int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, voi
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ stepping without allocation
+
+// Per-agent scratch (winner tags of the infection pass) for arbo_sim_step_noalloc: a fixed array
+// in the library's device image instead of memory allocated at run time. Host code must not use
+// the symbol as an address; it looks the device address up per device.
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[ARBO_NOALLOC_MAX_AGENTS];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kNoallocMaxDevices = 64;
+unsigned long long* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of the scratch array on `device` (which must be current); looked up once.
+int noalloc_scratch(int device, unsigned long long** out)
+{
+    if (device < 0 || device >= kNoallocMaxDevices) return fail(ARBO_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(ARBO_ERR_CUDA, std::string("cudaGetSymbolAddress of the no-allocation scratch: ") +
+                                           cudaGetErrorString(e));
+        g_noalloc_ptr[device] = (unsigned long long*)p;
+    }
+    *out = g_noalloc_ptr[device];
+    return ARBO_OK;
+}
+}  // namespace
+
+extern "C" int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream)
+{
+    if (!s) return fail(ARBO_ERR_INVALID, "null handle");
+    if (!s->inited) return fail(ARBO_ERR_STATE, "arbo_sim_step_noalloc before arbo_sim_init");
+    const size_t Np = (size_t)s->d.nvec * 4, Mp = (size_t)s->d.tiles * kTile;
+    if (Np + Mp > ARBO_NOALLOC_MAX_AGENTS)
+        return fail(ARBO_ERR_INVALID, "arbo_sim_step_noalloc: " + std::to_string(Np + Mp) +
+                                          " padded agents exceed ARBO_NOALLOC_MAX_AGENTS (" +
+                                          std::to_string(ARBO_NOALLOC_MAX_AGENTS) + ")");
+    CUDA_TRY(cudaSetDevice(s->device));
+    unsigned long long* scratch = nullptr;
+    int e = noalloc_scratch(s->device, &scratch);
+    if (e) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t n = std::min(nsteps, s->d.T - s->host_t);
+    if (n == 0) return ARBO_OK;
+    // Bids left in the shared array by any earlier call must not be read as current ones.
+    CUDA_TRY(cudaMemsetAsync(scratch, 0xFF, (Np + Mp) * sizeof(unsigned long long), st));
+    Dev d = s->d;
+    d.winh = scratch;
+    d.winm = scratch + Np;
+    for (uint32_t k = 0; k < n; ++k) {
+        e = launch_step(d, s->l, st, nullptr, 0);
+        if (!e) e = launch_advance(d, 1, st);
+        if (e) return fail(ARBO_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)e));
+        s->host_t += 1;
+    }
+    return ARBO_OK;
+}

@@ -323,6 +323,40 @@ int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, v
  * out has max_week entries. */
 int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, void* stream);
 
+/* ------------------------------------------------------------------ stepping without allocation */
+
+/* Most that arbo_sim_step_noalloc accepts: humans plus mosquito slots of a handle, each species
+ * rounded up to its padded length (humans to a multiple of 4, mosquito slots to whole 128-slot
+ * tiles). The scratch behind it is 8 bytes per agent, 16 MiB in all. */
+#define ARBO_NOALLOC_MAX_AGENTS (1u << 21)
+
+/*
+ * arbo_sim_step_noalloc — advance nsteps time steps like arbo_sim_step, but without allocating
+ * anything on the device or in the CUDA runtime. No counterpart in the reference: its host code
+ * always allocated fresh device buffers before each MCMC step (cpp/main.cpp:198-249).
+ *
+ * Who needs it: callers that hold a handle created earlier but must not allocate while they step
+ * it — a step loop running under a framework whose memory pool owns the device, an embedded or
+ * real-time driver that forbids allocation after set-up, or code that must not trigger the device
+ * memory that building a CUDA graph can take. arbo_sim_step captures and instantiates CUDA graphs
+ * on first use, and the handle's own per-agent scratch was allocated at create; this entry point
+ * launches the same step kernels one by one and takes the infection pass's per-agent scratch from
+ * a fixed array compiled into the library instead.
+ *
+ * Limits and behaviour:
+ *  - The handle's padded humans plus padded mosquito slots must not exceed ARBO_NOALLOC_MAX_AGENTS;
+ *    larger handles are rejected with ARBO_ERR_INVALID before anything is launched.
+ *  - The scratch array lives in the library's device image, so every GPU that loads the library
+ *    holds its 16 MiB until the process exits.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+ *    that device current; make that first call outside any stream capture.
+ *  - All calls, from every handle and thread, share the one array. Each call clears it (a memset on
+ *    `stream`) before its first step, so nothing left by an earlier call leaks into the results;
+ *    two calls whose work overlaps on the GPU (different streams, no ordering) race on it.
+ * Results are identical to arbo_sim_step's for the same handle state.
+ */
+int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream);
+
 /* ------------------------------------------------------------------ self-tests */
 
 /* Evaluate the device Philox4x32-10 on n (counter[4], key[2]) records packed as 6 uint32 each
