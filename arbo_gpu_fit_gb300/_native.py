@@ -32,7 +32,7 @@ class SimParamStruct(ctypes.Structure):
 
 
 ARCH_FIELDS = ["threadsPerWarp", "warpsPerSM", "totalSM", "demogBlock", "demogUnroll", "foiBlock", "infectBlock",
-               "graphSteps"]
+               "graphSteps", "demogPipeline"]
 
 
 class ArchParamStruct(ctypes.Structure):
@@ -56,6 +56,7 @@ QUIRK_SEED_DEAD_MOSQUITO = 0x2
 QUIRKS_REFERENCE = 0x3
 DEVERR_EVENT_OVERFLOW = 0x1
 DEVERR_COUNTER = 0x2
+DEVERR_STALL = 0x4
 
 SERIES = {"n_incidence": 0, "n_infected": 1, "one_subpop": 2, "n_count": 3, "m_count": 4, "m_infected": 5,
           "infected_subpop": 6}

@@ -174,6 +174,7 @@ int arbo_arch_param_query(arbo_arch_param* a, int device)
     a->foiBlock = 256;
     a->infectBlock = 256;
     a->graphSteps = 64;
+    a->demogPipeline = 0;
     int n = 0;
     if (device >= 0 && cudaGetDeviceCount(&n) == cudaSuccess && device < n) {
         int v = 0;
@@ -338,6 +339,13 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         minv[k] = a;
     }
     minv[4097] = (uint32_t)cdfm.size();
+    std::vector<uint32_t> minvh(65538);
+    for (uint32_t k = 0, a = 0; k <= 65536; ++k) {
+        const float thr = (float)k / 65536.0f;
+        while (a < cdfh.size() && cdfh[a] < thr) ++a;
+        minvh[k] = a;
+    }
+    minvh[65537] = (uint32_t)cdfh.size();
     std::vector<float> survh(p.nMaxInitialAgeYears + 1), survm(p.mMaxInitialAge + 1);
     survh[0] = 1.0f - table_at(cdfh, 0);
     for (uint32_t y = 1; y <= p.nMaxInitialAgeYears; ++y) survh[y] = survh[y - 1] + (1.0f - table_at(cdfh, 365u * y));
@@ -397,7 +405,8 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         {(void**)&d.msize, P * 4}, {(void**)&d.tcomm, (size_t)d.tiles * 4}, {(void**)&d.csr_loc, (P + 1) * 4},
         {(void**)&d.csr_to, std::max<size_t>(csr->nnz, 1) * 4}, {(void**)&d.infh, SP * 4}, {(void**)&d.infm, SP * 4},
         {(void**)&d.inc, SP * 4}, {(void**)&d.ncnt, P * 4}, {(void**)&d.mcnt, P * 4}, {(void**)&d.transh, SP * 4},
-        {(void**)&d.transm, SP * 4}, {(void**)&d.cdfh, cdfh.size() * 4}, {(void**)&d.cdfm, cdfm.size() * 4}, {(void**)&d.minv, minv.size() * 4},
+        {(void**)&d.transm, SP * 4}, {(void**)&d.cdfh, cdfh.size() * 4}, {(void**)&d.cdfm, cdfm.size() * 4}, {(void**)&d.minv, minv.size() * 4}, {(void**)&d.minvh, minvh.size() * 4},
+        {(void**)&d.hcomm, (size_t)((N + 127) / 128) * 4},
         {(void**)&d.survh, survh.size() * 4}, {(void**)&d.survm, survm.size() * 4}, {(void**)&d.etab, R * 4},
         {(void**)&d.winh, Np * 8}, {(void**)&d.winm, Mp * 8}, {(void**)&d.s_ninc, R * S * 4},
         {(void**)&d.s_ninf, R * S * 4}, {(void**)&d.s_one, R * S * 4}, {(void**)&d.s_ncount, R * 4},
@@ -442,6 +451,10 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     UP(d.cdfh, cdfh.data(), cdfh.size() * 4);
     UP(d.cdfm, cdfm.data(), cdfm.size() * 4);
     UP(d.minv, minv.data(), minv.size() * 4);
+    UP(d.minvh, minvh.data(), minvh.size() * 4);
+    std::vector<uint32_t> hcomm((N + 127) / 128);
+    for (uint32_t b = 0; b < hcomm.size(); ++b) hcomm[b] = comm_of_host(s->nloc, P, b * 128);
+    UP(d.hcomm, hcomm.data(), hcomm.size() * 4);
     UP(d.survh, survh.data(), survh.size() * 4);
     UP(d.survm, survm.data(), survm.size() * 4);
     UP(d.etab, s->etab.data(), R * 4);
@@ -461,6 +474,11 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     s->l.infectBlock = arch.infectBlock;
     s->l.numSM = arch.totalSM;
     s->l.demogBlocksPerSM = (uint32_t)demog_blocks_per_sm(arch.demogUnroll, arch.demogBlock);
+    cudaGetLastError();
+    s->l.pdl = 1;
+    s->l.demogPipeline = arch.demogPipeline ? 1u : 0u;
+    s->l.demogTmaBlocksPerSM = (uint32_t)demog_tma_blocks_per_sm(arch.demogUnroll);
+    cudaGetLastError();
     if (cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking) != cudaSuccess)
         return fail_free(fail(ARBO_ERR_CUDA, "cudaStreamCreate"));
     for (int k = 0; k < 4; ++k)

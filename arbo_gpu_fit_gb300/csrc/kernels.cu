@@ -45,21 +45,6 @@ __device__ __forceinline__ float cdf_at(const float* __restrict__ t, uint32_t n,
     return __ldg(&t[i < n ? i : n - 1]);
 }
 
-// First age whose CDF reaches ple: the death test "ple <= CDF(age)" of the reference
-// (cpp/ndemographic.cu:62, cpp/mdemographic.cu:72) holds exactly when age >= this value,
-// because the CDF table is non-decreasing. Evaluated once per birth instead of a table
-// gather (or powf/expf) per agent per step.
-__device__ int32_t death_age(const float* __restrict__ t, uint32_t n, float ple)
-{
-    if (!(__ldg(&t[n - 1]) >= ple)) return INT_MAX;
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&t[mid]) >= ple) hi = mid; else lo = mid + 1;
-    }
-    return (int32_t)lo;
-}
-
 __device__ __forceinline__ uint32_t lower_bound_f(const float* __restrict__ t, uint32_t n, float v)
 {
     // First index with t[index] >= v (n-1 if none): the first age whose cumulative survival
@@ -71,6 +56,12 @@ __device__ __forceinline__ uint32_t lower_bound_f(const float* __restrict__ t, u
     }
     return lo;
 }
+
+// Programmatic dependent launch: wait for the previous kernel of the stream (its memory is
+// visible afterwards), and let the next kernel of the stream start its prologue early. Both are
+// no-ops when the kernels are launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
 __device__ __forceinline__ Key load_key(const Ctrl* c)
 {
@@ -93,24 +84,52 @@ __device__ __forceinline__ unsigned long long order_key(uint32_t hiword, uint32_
 
 // ------------------------------------------------------------------ demographic pass
 
+// First age whose CDF reaches ple: the death test "ple <= CDF(age)" of the reference
+// (cpp/ndemographic.cu:62, cpp/mdemographic.cu:72) holds exactly when age >= this value, because
+// the CDF table is non-decreasing; it is evaluated once per birth instead of a table gather (or
+// powf/expf) per agent per step. Inverse bucket table of 2^bits + 2 entries: with
+// j = floor(ple * 2^bits), minv[j] (first age with CDF >= j / 2^bits) and minv[j+1] bracket the
+// answer, so a short binary search between them is exact. minv[2^bits + 1] = table size (none).
+__device__ __forceinline__ int32_t death_age_inv(const float* __restrict__ cdf, const uint32_t* __restrict__ minv,
+                                                 uint32_t n, float ple, float scale)
+{
+    const uint32_t j = (uint32_t)(ple * scale);
+    uint32_t lo = __ldg(&minv[j]), hi = __ldg(&minv[j + 1]);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&cdf[mid]) >= ple) hi = mid; else lo = mid + 1;
+    }
+    return lo >= n ? INT_MAX : (int32_t)lo;
+}
+
+// Community of human i: start from the community of its 128-agent block and walk forward.
+__device__ __forceinline__ uint32_t human_comm(const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ hcomm,
+                                               uint32_t P, uint32_t i)
+{
+    uint32_t c = __ldg(&hcomm[i >> 7]);
+    while (c + 1 < P && __ldg(&nloc[c + 1]) <= i) ++c;
+    return c;
+}
+
 // Rare per-human path: a transition of an infected human or a death with rebirth.
 // Returns the new status byte, with bit 8 set when the human died (its age restarts at 0).
 __device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, int32_t dage, uint32_t t,
-                                            const uint32_t* __restrict__ nloc, uint32_t P, const int32_t* n_exposed,
-                                            const int32_t* n_recovery, const uint8_t* n_strain, float* n_ple,
-                                            int32_t* n_dage, uint8_t* n_imm, uint32_t* infh, uint32_t* inc,
-                                            const float* __restrict__ cdfh, uint32_t ah, Key key, Ctrl* ctrl)
+                                            const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ hcomm,
+                                            uint32_t P, const int32_t* n_exposed, const int32_t* n_recovery,
+                                            const uint8_t* n_strain, float* n_ple, int32_t* n_dage, uint8_t* n_imm,
+                                            uint32_t* infh, uint32_t* inc, const float* __restrict__ cdfh,
+                                            const uint32_t* __restrict__ minvh, uint32_t ah, Key key, Ctrl* ctrl)
 {
     if (a < dage) {
         if (st == 2) {
             if (n_recovery[i] < a) {
-                const uint32_t c = comm_of(nloc, P, i);
+                const uint32_t c = human_comm(nloc, hcomm, P, i);
                 counter_dec(&infh[n_strain[i] * P + c], ctrl);
                 return 0;
             }
         } else if (st == 1) {
             if (n_exposed[i] < a) {
-                const uint32_t c = comm_of(nloc, P, i);
+                const uint32_t c = human_comm(nloc, hcomm, P, i);
                 const uint32_t s = n_strain[i];
                 atomicAdd(&inc[s * P + c], 1u);
                 atomicAdd(&infh[s * P + c], 1u);
@@ -120,13 +139,13 @@ __device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, 
         return st;
     }
     if (st == 2) {
-        const uint32_t c = comm_of(nloc, P, i);
+        const uint32_t c = human_comm(nloc, hcomm, P, i);
         counter_dec(&infh[n_strain[i] * P + c], ctrl);
     }
     const U4 r = draw4(key, kHumanRebirth, i >> 2, t);
     const float ple = u01(r.v[i & 3]);
     n_ple[i] = ple;
-    n_dage[i] = death_age(cdfh, ah, ple);
+    n_dage[i] = death_age_inv(cdfh, minvh, ah, ple, 65536.0f);
     n_imm[i] = 0;
     return 0x100u;
 }
@@ -163,9 +182,9 @@ __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32
                 continue;
             }
             if (st == 0 && a[k] < dd[k]) continue;  // susceptible survivor: ageing only
-            const uint32_t res = human_slow(4 * g + k, st, a[k], dd[k], t, d.nloc, d.P, d.n_exposed, d.n_recovery,
-                                            d.n_strain, d.n_ple, d.n_dage, d.n_imm, d.infh, d.inc, d.cdfh, d.ah,
-                                            key, d.ctrl);
+            const uint32_t res = human_slow(4 * g + k, st, a[k], dd[k], t, d.nloc, d.hcomm, d.P, d.n_exposed,
+                                            d.n_recovery, d.n_strain, d.n_ple, d.n_dage, d.n_imm, d.infh, d.inc,
+                                            d.cdfh, d.minvh, d.ah, key, d.ctrl);
             if (res & 0x100u) a[k] = 0;
             nsw = (nsw & ~(0xFFu << (8 * k))) | ((res & 0xFFu) << (8 * k));
         }
@@ -189,21 +208,6 @@ __device__ __noinline__ void mosq_counter(uint32_t* infm, const uint8_t* m_strai
     while (c + 1 < P && __ldg(&mloc[c + 1]) <= i) ++c;
     uint32_t* p = &infm[m_strain[i] * P + c];
     if (add > 0) atomicAdd(p, 1u); else counter_dec(p, ctrl);
-}
-
-// First age whose mosquito CDF reaches ple, via the inverse bucket table: with
-// j = floor(ple * 4096), minv[j] (first age with CDF >= j/4096) and minv[j+1] bracket the
-// answer, so a short binary search between them is exact. minv[4097] = table size (none).
-__device__ __forceinline__ int32_t death_age_m(const float* __restrict__ cdf, const uint32_t* __restrict__ minv,
-                                               uint32_t n, float ple)
-{
-    const uint32_t j = (uint32_t)(ple * 4096.0f);
-    uint32_t lo = __ldg(&minv[j]), hi = __ldg(&minv[j + 1]);
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&cdf[mid]) >= ple) hi = mid; else lo = mid + 1;
-    }
-    return lo >= n ? INT_MAX : (int32_t)lo;
 }
 
 constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
@@ -262,25 +266,11 @@ __device__ __forceinline__ uint32_t keep_low(uint32_t mask, uint32_t m)
 // slots and post each reborn slot's offset under its rank; one lane per group of four reborn
 // slots then draws the group, and one lane per reborn slot writes the newborn's age, PLE and
 // death age.
-__device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key, uint32_t q, uint32_t lane, uint32_t t,
-                                                    QuadSmem& sm)
+__device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, uint32_t q, uint32_t lane, uint32_t t,
+                                                   QuadSmem& sm, uint32_t (&SW)[kQuad], int4 (&A)[kQuad],
+                                                   const int4 (&D)[kQuad])
 {
     const uint32_t b0 = q * kQuad;
-    uint32_t SW[kQuad];
-    int4 A[kQuad], D[kQuad];
-#pragma unroll
-    for (uint32_t u = 0; u < kQuad; ++u) {
-        if (b0 + u < d.tiles) {
-            const uint32_t g = (b0 + u) * 32 + lane;
-            SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.m_state) + g);
-            A[u] = reinterpret_cast<const int4*>(d.m_age)[g];
-            D[u] = __ldcs(reinterpret_cast<const int4*>(d.m_dage) + g);
-        } else {
-            SW[u] = 0xFFFFFFFFu;
-            A[u] = make_int4(0, 0, 0, 0);
-            D[u] = A[u];
-        }
-    }
     const uint32_t bl = b0 + lane;
     const bool tile_lane = lane < kQuad && bl < d.tiles;
     const int32_t led = tile_lane ? d.ledger[bl] : 0;
@@ -294,17 +284,16 @@ __device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key,
 #pragma unroll
     for (uint32_t u = 0; u < kQuad; ++u) {
         const uint32_t sw = SW[u];
-        // Byte-parallel masks of the four state bytes (bit 7 of a byte: dead or padding).
+        // Byte-parallel masks of the four state bytes (bit 7 of a byte: dead or padding; padding
+        // bytes, 0xFF, exist only in the last tile).
         const uint32_t alive4 = ~sw & 0x80808080u;
-        const uint32_t pad4 = __vcmpeq4(sw, 0xFFFFFFFFu);
-        const uint32_t dead4 = sw & 0x80808080u & ~pad4;
-        int32_t a[4] = {A[u].x + (int32_t)((alive4 >> 7) & 1u), A[u].y + (int32_t)((alive4 >> 15) & 1u),
-                        A[u].z + (int32_t)((alive4 >> 23) & 1u), A[u].w + (int32_t)(alive4 >> 31)};
-        uint32_t dim = 0;
-        dim |= ((alive4 & 0x00000080u) && a[0] >= D[u].x) ? 1u : 0u;
-        dim |= ((alive4 & 0x00008000u) && a[1] >= D[u].y) ? 2u : 0u;
-        dim |= ((alive4 & 0x00800000u) && a[2] >= D[u].z) ? 4u : 0u;
-        dim |= ((alive4 & 0x80000000u) && a[3] >= D[u].w) ? 8u : 0u;
+        uint32_t dead4 = sw & 0x80808080u;
+        if (b0 + u == d.tiles - 1) dead4 &= ~__vcmpeq4(sw, 0xFFFFFFFFu);
+        const uint32_t al0 = (alive4 >> 7) & 1u, al1 = (alive4 >> 15) & 1u, al2 = (alive4 >> 23) & 1u,
+                       al3 = alive4 >> 31;
+        int32_t a[4] = {A[u].x + (int32_t)al0, A[u].y + (int32_t)al1, A[u].z + (int32_t)al2, A[u].w + (int32_t)al3};
+        const uint32_t dim = (al0 & (uint32_t)(a[0] >= D[u].x)) | ((al1 & (uint32_t)(a[1] >= D[u].y)) << 1) |
+                             ((al2 & (uint32_t)(a[2] >= D[u].z)) << 2) | ((al3 & (uint32_t)(a[3] >= D[u].w)) << 3);
         const uint32_t dm = nibble7(dead4) | dim;
         const uint32_t stat4 = sw & 0x03030303u;
         uint32_t rm = nibble7(((stat4 | (stat4 >> 1)) & (alive4 >> 7)) << 7);
@@ -433,14 +422,169 @@ __device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key,
         const uint32_t c = r & 3u;
         const float ple = u01(c == 0 ? v4.x : c == 1 ? v4.y : c == 2 ? v4.z : v4.w);
         d.m_ple[i] = ple;
-        d.m_dage[i] = death_age_m(d.cdfm, d.minv, d.am, ple);
+        d.m_dage[i] = death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f);
         d.m_age[i] = 0;
     }
     __syncwarp();
 }
 
+// Quad with its census words loaded straight from global memory.
+__device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key, uint32_t q, uint32_t lane, uint32_t t,
+                                                    QuadSmem& sm)
+{
+    const uint32_t b0 = q * kQuad;
+    uint32_t SW[kQuad];
+    int4 A[kQuad], D[kQuad];
+#pragma unroll
+    for (uint32_t u = 0; u < kQuad; ++u) {
+        if (b0 + u < d.tiles) {
+            const uint32_t g = (b0 + u) * 32 + lane;
+            SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.m_state) + g);
+            A[u] = reinterpret_cast<const int4*>(d.m_age)[g];
+            D[u] = __ldcs(reinterpret_cast<const int4*>(d.m_dage) + g);
+        } else {
+            SW[u] = 0xFFFFFFFFu;
+            A[u] = make_int4(0, 0, 0, 0);
+            D[u] = A[u];
+        }
+    }
+    mosquito_quad_core(d, key, q, lane, t, sm, SW, A, D);
+}
+
+// ------------------------------------------------------------------ TMA-staged pipeline
+
+// One warp's double buffer of quad census words, filled by bulk asynchronous copies.
+struct MosqStage {
+    uint32_t state[kQuad * 32];
+    int4 age[kQuad * 32];
+    int4 dage[kQuad * 32];
+};
+struct TmaWarpSmem {
+    MosqStage stage[2];
+    QuadSmem qs;
+    unsigned long long mbar[2];
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// One arrival that also announces `bytes` of asynchronous transfers for the current phase.
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16) completing on bar.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Waits for the phase of `bar` with the given parity; gives up after a bounded number of polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Lane 0 starts the three copies of quad q into `st`.
+__device__ __forceinline__ void issue_quad(const Dev& d, uint32_t q, MosqStage& st, unsigned long long* bar)
+{
+    const uint32_t b0 = q * kQuad;
+    const uint32_t nt = min(kQuad, d.tiles - b0);
+    // Order the warp's earlier generic reads of this buffer before the asynchronous writes.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, nt * kTile * 9);
+    bulk_load(st.state, d.m_state + (size_t)b0 * kTile, nt * kTile, bar);
+    bulk_load(st.age, d.m_age + (size_t)b0 * kTile, nt * kTile * 4, bar);
+    bulk_load(st.dage, d.m_dage + (size_t)b0 * kTile, nt * kTile * 4, bar);
+}
+
+// Persistent demographic pass with TMA staging. Every warp first walks chunks of 32*U human
+// groups (grid-stride), then its mosquito quads: lane 0 starts the bulk copy of the warp's next
+// quad into the other half of its double buffer before the current quad is processed, so the
+// census streams of all warps overlap with their arithmetic. Waits are bounded: on a timeout the
+// kernel records ARBO_DEVERR_STALL, waits (bounded) for its own copy in flight and stops.
 template <int U>
-__global__ void __launch_bounds__(256) k_demog(Dev d, uint32_t hblocks, uint32_t koff)
+__global__ void __launch_bounds__(128, 4) k_demog_tma(Dev d, uint32_t koff)
+{
+    __shared__ TmaWarpSmem ws_all[4];
+    const uint32_t t = d.ctrl->t + koff;
+    const Key key = load_key(d.ctrl);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t gw = blockIdx.x * (blockDim.x >> 5) + warp, nw = gridDim.x * (blockDim.x >> 5);
+    TmaWarpSmem& ws = ws_all[warp];
+    const uint32_t quads = (d.tiles + kQuad - 1) / kQuad;
+    if (lane == 0) {
+        mbar_init(&ws.mbar[0], 1);
+        mbar_init(&ws.mbar[1], 1);
+        mbar_fence_init();
+        if (gw < quads) issue_quad(d, gw, ws.stage[0], &ws.mbar[0]);
+    }
+    __syncwarp();
+    const uint32_t hchunks = (d.nvec + 32 * U - 1) / (32 * U);
+    for (uint32_t ch = gw; ch < hchunks; ch += nw) demog_humans<U>(d, key, ch * 32 * U + lane, 32, t);
+    uint32_t phase = 0;  // bit s: parity to wait for on stage s
+    uint32_t i = 0;
+    for (uint32_t q = gw; q < quads; q += nw, ++i) {
+        const uint32_t sidx = i & 1u;
+        const uint32_t nq = q + nw;
+        if (lane == 0 && nq < quads) issue_quad(d, nq, ws.stage[sidx ^ 1u], &ws.mbar[sidx ^ 1u]);
+        const bool ok = mbar_wait(&ws.mbar[sidx], (phase >> sidx) & 1u);
+        phase ^= 1u << sidx;
+        if (!__all_sync(kFull, ok)) {
+            if (lane == 0) {
+                atomicOr(&d.ctrl->err, ARBO_DEVERR_STALL);
+                if (nq < quads) mbar_wait(&ws.mbar[sidx ^ 1u], (phase >> (sidx ^ 1u)) & 1u);
+            }
+            break;
+        }
+        const MosqStage& st = ws.stage[sidx];
+        const uint32_t b0 = q * kQuad;
+        uint32_t SW[kQuad];
+        int4 A[kQuad], D[kQuad];
+#pragma unroll
+        for (uint32_t u = 0; u < kQuad; ++u) {
+            if (b0 + u < d.tiles) {
+                SW[u] = st.state[u * 32 + lane];
+                A[u] = st.age[u * 32 + lane];
+                D[u] = st.dage[u * 32 + lane];
+            } else {
+                SW[u] = 0xFFFFFFFFu;
+                A[u] = make_int4(0, 0, 0, 0);
+                D[u] = A[u];
+            }
+        }
+        __syncwarp();  // every lane has its words before the buffer is refilled next iteration
+        mosquito_quad_core(d, key, q, lane, t, ws.qs, SW, A, D);
+    }
+    griddep_launch_dependents();
+}
+
+template <int U>
+__global__ void __launch_bounds__(256, 4) k_demog(Dev d, uint32_t hblocks, uint32_t koff)
 {
     __shared__ QuadSmem wsm[8];
     const uint32_t t = d.ctrl->t + koff;
@@ -453,6 +597,7 @@ __global__ void __launch_bounds__(256) k_demog(Dev d, uint32_t hblocks, uint32_t
         const uint32_t q = (blockIdx.x - hblocks) * wpb + warp;
         if (q * kQuad < d.tiles) demog_mosquito_quad(d, key, q, lane, t, wsm[warp]);
     }
+    griddep_launch_dependents();
 }
 
 // ------------------------------------------------------------------ series + force of infection
@@ -489,6 +634,7 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
 {
     __shared__ uint32_t s_cnt[512], s_scan[513], s_loc[128], s_deg[128], s_sum[3 * ARBO_MAX_STRAINS + 2],
         s_wt[16];
+    __shared__ uint32_t s_to[128][8];  // CSR row of each pair's source community (degree <= 8)
     const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
     const uint32_t row = collect_only ? 0u : t + 1;
@@ -502,16 +648,21 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
     if (tid < K) {
         const uint32_t p = p0 + tid;
         if (p < SP) {
-            // Every independent load and draw first, then the arithmetic.
+            // Loads of static data and the keyed draws run before the wait on the demographic
+            // kernel (programmatic dependent launch); the counters it writes are read after.
             const uint32_t s = p / P, c = p - s * P;
-            const uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
-            const uint32_t ncc = __ldg(&d.ncnt[c]), mcc = d.mcnt[c];
+            const uint32_t ncc = __ldg(&d.ncnt[c]);
             const uint32_t loc = __ldg(&d.csr_loc[c]), loc1 = __ldg(&d.csr_loc[c + 1]);
+            if (!collect_only && loc1 - loc <= 8)
+                for (uint32_t q = 0; q < loc1 - loc; ++q) s_to[tid][q] = __ldg(&d.csr_to[loc + q]);
             U4 rh, rm;
             if (!collect_only) {
                 rh = draw4(key, kFoiHM, p, t);
                 rm = draw4(key, kFoiMH, p, t);
             }
+            griddep_wait();
+            const uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
+            const uint32_t mcc = d.mcnt[c];
             if (ic) d.inc[p] = 0u;
             if (ih) atomicAdd(&s_sum[s], ih);
             if (ic) atomicAdd(&s_sum[ARBO_MAX_STRAINS + s], ic);
@@ -541,6 +692,7 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
             }
         }
     }
+    griddep_wait();
     // s_cnt[4*pair + kind] for kind 0 HM local, 1 HM long, 2 MH local, 3 MH long
     if (tid < K) {
 #pragma unroll
@@ -557,6 +709,7 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
         if (s_sum[3 * ARBO_MAX_STRAINS + 1]) atomicAdd(&d.s_mcount[row], s_sum[3 * ARBO_MAX_STRAINS + 1]);
     }
     if (collect_only) return;
+    griddep_launch_dependents();
     // Exclusive scan of the groups of four events of every (pair, kind) entry.
     uint32_t v = (s_cnt[tid] + 3) >> 2;
     const uint32_t own = v;
@@ -597,7 +750,8 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
 #pragma unroll
         for (int qq = 0; qq < 4; ++qq) {
             if (4 * r4 + qq >= n) break;
-            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : __ldg(&d.csr_to[loc + bounded(r.v[qq], deg)]);
+            const uint32_t nb = (kind & 1u) ? 0u : bounded(r.v[qq], deg);
+            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : (deg <= 8 ? s_to[pair][nb] : __ldg(&d.csr_to[loc + nb]));
             atomicAdd(&trans[s * P + dest], 1u);
         }
     }
@@ -616,25 +770,32 @@ __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t 
 }
 
 // Target of mosquito event e: the first alive slot of its attempt sequence (dead slots are
-// retried, cpp/mepidemic.cu:206-235). Returns UINT_MAX when the attempts run out.
+// retried, cpp/mepidemic.cu:206-235). Returns UINT_MAX when the attempts run out. The four
+// candidates of one Philox call are loaded together (one memory round trip) and the first alive
+// one in attempt order is taken.
 __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key, uint32_t pidx, uint32_t e,
                                                     uint32_t base, uint32_t size, uint32_t t)
 {
     for (uint32_t a = 0; a < d.maxTarget; a += 4) {
         const U4 r = draw4(key, kInfMTarget, pidx, t, e, a >> 2);
+        uint32_t slot[4], st[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (a + q >= d.maxTarget) break;
-            const uint32_t slot = base + bounded(r.v[q], size);
-            if (!(__ldcg(&d.m_state[slot]) & kDead)) return slot;
-        }
+        for (int q = 0; q < 4; ++q) slot[q] = base + bounded(r.v[q], size);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) st[q] = (a + q < d.maxTarget) ? __ldcg(&d.m_state[slot[q]]) : (uint32_t)kDead;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (!(st[q] & kDead)) return slot[q];
     }
     return UINT_MAX;
 }
 
 // Per-CTA tables of the infection kernel: the CTA's K communities (one per warp) and their
 // events of every serotype flattened into one index space.
+constexpr uint32_t kTargetCache = 1024;  // items whose targets Phase A keeps for Phase C
+
 struct InfectSmem {
+    uint4 target[kTargetCache];          // per item: four human targets, or a mosquito slot in .x
     uint32_t cstart[17];                 // flattened item start of each community (K+1)
     uint32_t hstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, human groups
     uint32_t mstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, mosquito events
@@ -669,12 +830,13 @@ __device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, ui
     }
 }
 
-// Infection draws. A CTA of K warps owns K communities. Warp w reads its community's event
-// counts (lanes 0..S-1), draws its introduction counts and first serotypes in parallel lanes, and
-// posts the per-serotype tables; the events of the K communities (groups of four human events,
-// single mosquito events) then form one index space shared by all the CTA's threads:
+// Infection draws. A CTA of 64*K threads owns K communities. Warp w < K reads community w's
+// event counts (lanes 0..S-1), draws its introduction counts and first serotypes in parallel
+// lanes, and posts the per-serotype tables; the events of the K communities (groups of four
+// human events, single mosquito events) then form one index space shared by all the CTA's threads:
 //   A: every event whose target is eligible at the start of the pass bids its serial order
-//      (serotype position j, event index) for the target with atomicMin;
+//      (serotype position j, event index) for the target with atomicMin; the targets of the first
+//      kTargetCache items are kept in shared memory for phase C;
 //   B: external introductions (cpp/nepidemic.cu:261-309), per community in serial order, one warp
 //      testing 32 attempts at a time;
 //   C: each event that won its target applies its infection.
@@ -688,30 +850,36 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
     const uint32_t hiword = ~epoch;
     const Key key = load_key(d.ctrl);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = blockDim.x >> 5;
+    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
     const uint32_t S = d.S, P = d.P;
     const float ext = __fdiv_rn(d.extInf, (float)P);
 
     for (uint32_t cb = blockIdx.x * K; cb < P; cb += gridDim.x * K) {
         const uint32_t c = cb + warp;
+        const bool owner = warp < K && c < P;
         uint32_t ne = 0;
         uint32_t items = 0;
-        if (c < P) {
-            // Loads that do not depend on the step first, then the keyed draws.
+        if (owner) {
+            // Static loads and keyed draws first; the event counts and alive mosquitoes written by
+            // the previous kernels are read after the programmatic-launch wait.
             const uint32_t ns = __ldg(&d.nsize[c]);
             const uint32_t ms = __ldg(&d.msize[c]);
             const uint32_t nb0 = __ldg(&d.nloc[c]), mb0 = __ldg(&d.mloc[c]);
-            const uint32_t mc = d.mcnt[c];
             const uint32_t pl = lane * P + c;
+            U4 rd;
+            if (lane < S) rd = draw4(key, kIntroCount, pl, t);
+            else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
+            else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
+            griddep_wait();
+            const uint32_t mc = d.mcnt[c];
             uint32_t kh = lane < S ? d.transh[pl] : 0u;
             uint32_t km = lane < S ? d.transm[pl] : 0u;
             uint32_t sv = 0;
             if (lane < S) {
-                const U4 rn = draw4(key, kIntroCount, pl, t);
                 if (kh) d.transh[pl] = 0;
                 if (km) d.transm[pl] = 0;
                 if (ns == 0) kh = 0;
-                else ne = (uint32_t)resolve(ext, rn.v[0]);
+                else ne = (uint32_t)resolve(ext, rd.v[0]);
                 if (mc == 0) km = 0;
                 if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
                     atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
@@ -719,11 +887,9 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
                     km = min(km, kMaxEventsPerPair - 1);
                 }
             } else if (lane == 8) {
-                const U4 r = draw4(key, kInfMStart, c, t);
-                if (mc) sv = bounded(r.v[0], S);
+                if (mc) sv = bounded(rd.v[0], S);
             } else if (lane == 9) {
-                const U4 r = draw4(key, kInfHStart, c, t);
-                if (ns) sv = bounded(r.v[0], S);
+                if (ns) sv = bounded(rd.v[0], S);
             }
             const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
             uint32_t H = 0, Mt = 0;
@@ -751,8 +917,9 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
             }
             items = H + Mt;
         }
-        // Item starts of the K communities (warp totals, serial over at most 16 warps).
-        if (lane == 0) sh.cstart[warp + 1] = items;
+        griddep_wait();
+        // Item starts of the K communities (serial over at most 8 entries).
+        if (lane == 0 && warp < K) sh.cstart[warp + 1] = items;
         __syncthreads();
         if (tid == 0) {
             sh.cstart[0] = 0;
@@ -772,24 +939,28 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
             if (human) {
                 const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
                 const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+                uint32_t tg[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+                if (it < kTargetCache) sh.target[it] = make_uint4(tg[0], tg[1], tg[2], tg[3]);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const uint32_t e = 4 * idx + q;
                     if (e >= k) break;
-                    const uint32_t i = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
-                    const uint32_t st = d.n_status[i], im = d.n_imm[i];
-                    if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[i], order_key(hiword, j, 0, e));
+                    const uint32_t st = d.n_status[tg[q]], im = d.n_imm[tg[q]];
+                    if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[tg[q]], order_key(hiword, j, 0, e));
                 }
             } else {
                 const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
                 const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+                if (it < kTargetCache) sh.target[it].x = slot;
                 if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
                 else if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
             }
         }
         __syncthreads();
         // Phase B: warp w handles the introductions of its own community.
-        if (any_intro && c < P) {
+        if (any_intro && owner) {
             const uint32_t s0h = sh.s0h[warp], nbase = sh.nbase[warp], ns = sh.ns[warp];
             for (uint32_t j = 0; j < S; ++j) {
                 const uint32_t s = (s0h + j) % S, ph = s * P + c;
@@ -834,18 +1005,29 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
             const uint32_t cc = sh.c[w];
             if (human) {
                 const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
-                const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+                uint32_t tg[4];
+                if (it < kTargetCache) {
+                    const uint4 v = sh.target[it];
+                    tg[0] = v.x;
+                    tg[1] = v.y;
+                    tg[2] = v.z;
+                    tg[3] = v.w;
+                } else {
+                    const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+                }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const uint32_t e = 4 * idx + q;
                     if (e >= k) break;
-                    const uint32_t i = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
-                    if (__ldcg(&d.winh[i]) == order_key(hiword, j, 0, e))
-                        infect_human(d, i, s, draw4(key, kInfHExposed, ph, t, e));
+                    if (__ldcg(&d.winh[tg[q]]) == order_key(hiword, j, 0, e))
+                        infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e));
                 }
             } else {
                 const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
-                const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+                const uint32_t slot = it < kTargetCache ? sh.target[it].x
+                                                        : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
                 if (slot != UINT_MAX && __ldcg(&d.winm[slot]) == order_key(hiword, j, 0, idx)) {
                     const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
                     d.m_state[slot] = 1;
@@ -892,7 +1074,7 @@ __global__ void k_init_humans(Dev d)
         if (u01(dr[3 + s]) < d.seroPrev) imm |= 1u << s;
     d.n_age[j] = age;
     d.n_ple[j] = ple;
-    d.n_dage[j] = death_age(d.cdfh, d.ah, ple);
+    d.n_dage[j] = death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f);
     d.n_status[j] = 0;
     d.n_strain[j] = 0;
     d.n_imm[j] = (uint8_t)imm;
@@ -940,7 +1122,7 @@ __global__ void k_init_mosquitoes(Dev d)
             d.m_state[i] = 0;
             d.m_age[i] = (int32_t)a;
             d.m_ple[i] = ple;
-            d.m_dage[i] = death_age_m(d.cdfm, d.minv, d.am, ple);
+            d.m_dage[i] = death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f);
         }
     }
     const uint32_t tile_dead = __reduce_add_sync(kFull, ndead);
@@ -1027,9 +1209,30 @@ int demog_blocks_per_sm(uint32_t unroll, uint32_t block)
     return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
+int demog_tma_blocks_per_sm(uint32_t unroll)
+{
+    int n = 0;
+    cudaError_t e;
+    if (unroll == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_tma<4>, 128, 0);
+    else if (unroll == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_tma<2>, 128, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_tma<1>, 128, 0);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
 int launch_demog(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 {
     const uint32_t U = l.demogUnroll;
+    if (l.demogPipeline) {
+        const uint32_t quads = cdiv(d.tiles, kQuad);
+        const uint32_t hchunks = cdiv(d.nvec, 32 * U);
+        const uint32_t need = cdiv(quads > hchunks ? quads : hchunks, 4);
+        uint32_t grid = (l.numSM ? l.numSM : 152u) * (l.demogTmaBlocksPerSM ? l.demogTmaBlocksPerSM : 1u);
+        if (grid > need) grid = need;
+        if (U == 4) k_demog_tma<4><<<grid, 128, 0, st>>>(d, koff);
+        else if (U == 2) k_demog_tma<2><<<grid, 128, 0, st>>>(d, koff);
+        else k_demog_tma<1><<<grid, 128, 0, st>>>(d, koff);
+        return (int)cudaGetLastError();
+    }
     const uint32_t hblocks = cdiv(d.nvec, (uint64_t)l.demogBlock * U);
     const uint32_t quads = cdiv(d.tiles, kQuad);
     const uint32_t mblocks = cdiv(quads, l.demogBlock / 32);
@@ -1040,22 +1243,38 @@ int launch_demog(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
     return (int)cudaGetLastError();
 }
 
+// Launch with programmatic stream serialization: the kernel may start while the previous kernel
+// of the stream finishes; it calls griddepcontrol.wait before reading that kernel's results.
+template <typename... Args>
+static int launch_pdl(void (*kernel)(Args...), dim3 grid, dim3 block, cudaStream_t st, bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return (int)cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only, uint32_t koff)
 {
     const uint32_t SP = d.S * d.P;
     const uint32_t K = l.foiBlock / 4;
-    k_foi<<<cdiv(SP, K), l.foiBlock, 0, st>>>(d, collect_only, koff);
-    return (int)cudaGetLastError();
+    return launch_pdl(k_foi, dim3(cdiv(SP, K)), dim3(l.foiBlock), st, l.pdl && !collect_only, d, collect_only, koff);
 }
 
 int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 {
-    const uint32_t wpb = l.infectBlock / 32;
-    uint32_t blocks = cdiv(d.P, wpb);
+    const uint32_t per = l.infectBlock >= 64 ? l.infectBlock / 64 : 1u;
+    uint32_t blocks = cdiv(d.P, per);
     const uint32_t cap = 16u * (l.numSM ? l.numSM : 152u);
     if (blocks > cap) blocks = cap;
-    k_infect<<<blocks, l.infectBlock, 0, st>>>(d, koff);
-    return (int)cudaGetLastError();
+    return launch_pdl(k_infect, dim3(blocks), dim3(l.infectBlock), st, l.pdl != 0, d, koff);
 }
 
 int launch_init(const Dev& d, const Launch& l, void* stream)

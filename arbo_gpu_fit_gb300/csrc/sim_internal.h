@@ -68,6 +68,7 @@ struct Dev {
     uint32_t* nsize;  // [P]
     uint32_t* msize;  // [P]
     uint32_t* tcomm;  // [tiles] community of each mosquito tile's first slot
+    uint32_t* hcomm;  // [ceil(N/128)] community of each 128-human block's first agent
     uint32_t* csr_loc;
     uint32_t* csr_to;
     // counters
@@ -82,6 +83,7 @@ struct Dev {
     float* cdfh;
     float* cdfm;
     uint32_t* minv;   // [4098] first mosquito age with CDF >= k/4096 (table size if none)
+    uint32_t* minvh;  // [65538] first human age with CDF >= k/65536 (table size if none)
     float* survh;
     float* survm;
     float* etab;
@@ -101,12 +103,16 @@ struct Dev {
 
 struct Launch {
     uint32_t demogBlock, demogUnroll, foiBlock, infectBlock, numSM, demogBlocksPerSM;
+    uint32_t pdl;  // 1: k_foi and k_infect use programmatic dependent launch
+    uint32_t demogPipeline;       // 1: persistent TMA-staged demographic kernel
+    uint32_t demogTmaBlocksPerSM;
 };
 
 // Kernel launchers (kernels.cu). Each returns the cudaError_t of the launch as int.
 int launch_init(const Dev& d, const Launch& l, void* stream);
 // Resident CTAs per SM of the demographic kernel for the given unroll and block size.
 int demog_blocks_per_sm(uint32_t unroll, uint32_t block);
+int demog_tma_blocks_per_sm(uint32_t unroll);
 // One time step at offset koff from ctrl->t (the step counter advances only through
 // launch_advance); with events != null, records cudaEvent_t events[0..3] around the three kernels.
 int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint32_t koff);

@@ -39,6 +39,7 @@ extern "C" {
 /* Bits of the device error word (arbo_sim_status). */
 #define ARBO_DEVERR_EVENT_OVERFLOW 0x1u /* > 2^24 events for one (strain, community) in a step */
 #define ARBO_DEVERR_COUNTER 0x2u        /* a counter would have gone below zero               */
+#define ARBO_DEVERR_STALL 0x4u          /* a bounded wait for staged census data gave up      */
 
 #define ARBO_MAX_STRAINS 8u
 #define ARBO_MOSQUITO_TILE 128u /* logical recruitment tile (reference C_THREADSPERBLOCK) */
@@ -128,6 +129,8 @@ typedef struct arbo_arch_param {
     uint32_t foiBlock;       /* threads per CTA of the force-of-infection kernel           */
     uint32_t infectBlock;    /* threads per CTA of the infection kernel                    */
     uint32_t graphSteps;     /* steps captured per CUDA graph (0: no graph)                */
+    uint32_t demogPipeline;  /* 1: persistent demographic kernel with TMA-staged mosquito tiles
+                                (128-thread CTAs; demogBlock then unused), 0: one quad per warp */
 } arbo_arch_param;
 
 /* arbo_io_param — replaces IOParam (cpp/IOParam.h:10-25). Only odir is used (CSV output). */

@@ -17,9 +17,10 @@ from tests.helpers import compare_state, isolated_network, recount, small_case
 pytestmark = pytest.mark.gpu
 
 SHAPES = [
-    dict(demogBlock=256, demogUnroll=2, foiBlock=256, infectBlock=256, graphSteps=64),
-    dict(demogBlock=32, demogUnroll=1, foiBlock=32, infectBlock=32, graphSteps=0),
-    dict(demogBlock=128, demogUnroll=4, foiBlock=512, infectBlock=64, graphSteps=7),
+    dict(demogBlock=256, demogUnroll=2, foiBlock=256, infectBlock=256, graphSteps=64, demogPipeline=1),
+    dict(demogBlock=32, demogUnroll=1, foiBlock=32, infectBlock=32, graphSteps=0, demogPipeline=0),
+    dict(demogBlock=128, demogUnroll=4, foiBlock=512, infectBlock=64, graphSteps=7, demogPipeline=0),
+    dict(demogBlock=256, demogUnroll=1, foiBlock=128, infectBlock=512, graphSteps=3, demogPipeline=1),
 ]
 
 
@@ -63,7 +64,7 @@ def test_philox_equals_curand_philox(gpu):
         assert list(out[i]) == ob.philox([i, 0, 0, 0], [seed & 0xFFFFFFFF, seed >> 32])
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["default", "narrow-nograph", "wide-graph7"])
+@pytest.mark.parametrize("shape", SHAPES, ids=["default", "narrow-nograph", "wide-graph7", "tma-unroll1-graph3"])
 def test_parity_small_epidemic(gpu, shape):
     w = small_case()
     sim, orc = pair(w, shape)
