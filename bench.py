@@ -37,8 +37,10 @@ FLUSH_MB = 320
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # Per-launch DRAM traffic of the demographic kernel on this workload, from the ncu capture
-# summarised in profiles/k_demog_plain_large.md (None until captured).
-DEMOG_TRAFFIC_BYTES = None
+# summarised in profiles/k_demog_plain_large.md: dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch (65,444,864 + 6,548,992 bytes); part of the age writes is still dirty in L2 when the
+# kernel ends, so the write count is low.
+DEMOG_TRAFFIC_BYTES = 71_993_856
 
 
 def parse():
