@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--e2e-runs", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profile-sized workload (1/8 of the large one)")
+    ap.add_argument("--ref-gpu-steps", type=int, default=-1,
+                    help="steps of the reference's own CUDA kernels timed in the reference arm "
+                         "(-1: the same as --steps after --warmup untimed steps; 0: skip)")
     return ap.parse_args()
 
 
@@ -208,7 +211,41 @@ def reference_arm(args, world, rank):
         "e2e": {"value": rate, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference has no CPU implementation; its per-step logic restated serially in oracle/",
     }
+    if args.ref_gpu_steps != 0:
+        line["reference_cuda_kernels"] = reference_cuda_kernels(args, w)
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda_kernels(args, w):
+    """The reference's own CUDA kernels on this GPU: compiled from its sources for sm_103a
+    (oracle/ref_build.py) and launched as cpp/simulation.cpp launches them, dataCollect included
+    (oracle/ref_kernels.py). Same workload shape; community sizes drawn by the reference's own
+    assignment kernel with this workload's community weights. Reported beside the arm's CPU value."""
+    from oracle import ref_build
+
+    if not ref_build.prebuilt():
+        return {"unavailable": "reference cubins not built (oracle/ref_build.py needs the reference sources)"}
+    try:
+        from tests.distribution import expected_series
+        from oracle.ref_kernels import ReferenceKernels
+
+        sp = w.parameter.simulation
+        K = args.steps if args.ref_gpu_steps < 0 else args.ref_gpu_steps
+        W = args.warmup
+        ref = ReferenceKernels(0)
+        ref.setup(sp, w.network.loc, w.network.to, w.network.weight, expected_series(sp, w.max_time),
+                  int(sp.nSize), int(sp.mSize), w.max_time, int(sp.nStrains), n_weights=w.n_sizes, m_weights=w.m_sizes)
+        ref.init(w.seed, collect=False)
+        r = ref.time_steps(K, W)
+        ref.drv.free_all()
+        sec = r["device_ms"] / 1e3
+        return {"value": w.agents * K / sec, "unit": "agent-steps/s", "ms_per_step": r["device_ms"] / K,
+                "steps": K, "warmup": W, "launches_per_step": r["launches_per_step"],
+                "timing": (f"steps recorded into CUDA graphs of {r['graph_steps']} steps, launched back to back "
+                           "between CUDA events on the launching stream; L2 not flushed"),
+                "kind": "reference CUDA kernels (sm_103a cubins from the reference sources)"}
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"[:300]}
 
 
 def ours_arm(args, world, rank, local):
