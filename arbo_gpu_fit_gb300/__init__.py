@@ -3,8 +3,8 @@
 The compute path is the native library ``_lib/libarbo_gb300.so`` (CUDA kernels + C-ABI,
 include/arbo.h); this package is the host-side mirror of the reference's interface.
 """
-from .simulation import (ArchitectureParam, IOParam, Network, Parameter, Simulation, SimulationParam,
+from .simulation import (ArchitectureParam, Batch, IOParam, Network, Parameter, Simulation, SimulationParam,
                          calc_cumulative_com_size, community_sizes, create_network, simulation)
 
-__all__ = ["ArchitectureParam", "IOParam", "Network", "Parameter", "Simulation", "SimulationParam",
+__all__ = ["ArchitectureParam", "Batch", "IOParam", "Network", "Parameter", "Simulation", "SimulationParam",
            "calc_cumulative_com_size", "community_sizes", "create_network", "simulation"]

@@ -100,6 +100,17 @@ SIGNATURES = {
     "arbo_sim_write_incidence": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
     "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
+    "arbo_batch_create": (c_int, [POINTER(c_void_p), c_uint32, POINTER(ArchParamStruct), POINTER(c_void_p)]),
+    "arbo_batch_destroy": (c_int, [c_void_p]),
+    "arbo_batch_size": (c_int, [c_void_p, POINTER(c_uint32), POINTER(c_uint64)]),
+    "arbo_batch_init": (c_int, [c_void_p, c_void_p]),
+    "arbo_batch_step": (c_int, [c_void_p, c_uint32, c_void_p]),
+    "arbo_batch_run": (c_int, [c_void_p, c_void_p]),
+    "arbo_batch_set_arch": (c_int, [c_void_p, POINTER(ArchParamStruct)]),
+    "arbo_batch_get_arch": (c_int, [c_void_p, POINTER(ArchParamStruct), POINTER(c_uint32)]),
+    "arbo_batch_autotune": (c_int, [c_void_p, c_uint32, POINTER(ArchParamStruct), POINTER(c_float), c_void_p]),
+    "arbo_batch_time_phases": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_float), c_void_p]),
+    "arbo_batch_time_steps": (c_int, [c_void_p, c_uint32, c_uint32, POINTER(c_float), c_void_p]),
     "arbo_selftest_philox": (c_int, [POINTER(c_uint32), c_uint32, POINTER(c_uint32)]),
     "arbo_selftest_curand_philox": (c_int, [c_uint64, c_uint32, POINTER(c_uint32)]),
 }

@@ -1069,3 +1069,434 @@ extern "C" int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream)
     }
     return ARBO_OK;
 }
+
+// ------------------------------------------------------------------ batches of simulations
+//
+// The reference runs its replicates and MCMC proposals one simulation at a time
+// (cpp/main.cpp:262-280). A batch steps many existing handles together: one persistent kernel
+// per phase walks the concatenated blocks of all instances, so small and uneven simulations fill
+// the GPU together. Every instance keeps its own buffers, key and step counter, and its results
+// are bit-identical to stepping it alone (the random stream is keyed, not launch-dependent).
+
+struct arbo_batch {
+    std::vector<arbo_sim*> sims;
+    int device = 0;
+    arbo_arch_param arch{};
+    Launch l{};
+    BatchDev bd{};
+    void* mem = nullptr;  // Dev[n] followed by the four offset tables
+    uint32_t blocks[3] = {0, 0, 0};
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t gmulti = nullptr, gone = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> step_ev;
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+};
+
+namespace {
+
+int arch_knobs_ok(const arbo_arch_param& a)
+{
+    return a.demogBlock >= 32 && a.demogBlock <= 256 && a.demogBlock % 32 == 0 &&
+           (a.demogUnroll == 1 || a.demogUnroll == 2 || a.demogUnroll == 4) && a.foiBlock >= 32 &&
+           a.foiBlock <= 512 && a.foiBlock % 32 == 0 && a.infectBlock >= 32 && a.infectBlock <= 512 &&
+           a.infectBlock % 32 == 0;
+}
+
+void batch_drop_graphs(arbo_batch* b)
+{
+    if (b->gmulti) cudaGraphExecDestroy(b->gmulti);
+    if (b->gone) cudaGraphExecDestroy(b->gone);
+    b->gmulti = b->gone = nullptr;
+}
+
+// Block counts of every instance for the launch shapes of `a`; descriptors and tables uploaded.
+int batch_configure(arbo_batch* b, const arbo_arch_param& a)
+{
+    if (!arch_knobs_ok(a))
+        return fail(ARBO_ERR_INVALID, "launch knobs: demogBlock in [32, 256], foiBlock and infectBlock in [32, 512], "
+                                      "all multiples of 32; demogUnroll 1, 2 or 4");
+    const uint32_t n = (uint32_t)b->sims.size();
+    Launch l{};
+    l.demogBlock = a.demogBlock;
+    l.demogUnroll = a.demogUnroll;
+    l.foiBlock = a.foiBlock;
+    l.infectBlock = a.infectBlock;
+    l.numSM = a.totalSM ? a.totalSM : 152u;
+    l.pdl = 1;
+    std::vector<uint32_t> demog_off(n + 1, 0), demog_h(n, 0), foi_off(n + 1, 0), infect_off(n + 1, 0);
+    const uint32_t K = a.infectBlock >= 64 ? a.infectBlock / 64 : 1u;
+    for (uint32_t i = 0; i < n; ++i) {
+        const Dev& d = b->sims[i]->d;
+        const uint64_t hb = cdiv(d.nvec, (uint64_t)a.demogBlock * a.demogUnroll);
+        const uint64_t mb = cdiv(cdiv(d.tiles, kQuad), a.demogBlock / 32);
+        const uint64_t fb = cdiv((uint64_t)d.S * d.P, a.foiBlock / 4);
+        const uint64_t ib = cdiv(d.P, K);
+        if (demog_off[i] + hb + mb >= (1ull << 31) || foi_off[i] + fb >= (1ull << 31) ||
+            infect_off[i] + ib >= (1ull << 31))
+            return fail(ARBO_ERR_INVALID, "batch too large: more than 2^31 blocks in one phase");
+        demog_h[i] = (uint32_t)hb;
+        demog_off[i + 1] = demog_off[i] + (uint32_t)(hb + mb);
+        foi_off[i + 1] = foi_off[i] + (uint32_t)fb;
+        infect_off[i + 1] = infect_off[i] + (uint32_t)ib;
+    }
+    uint32_t occ[3] = {1, 1, 1};
+    const int oe = batch_blocks_per_sm(l, occ);
+    if (oe) return fail(ARBO_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString((cudaError_t)oe));
+    const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3) * 4;
+    if (!b->mem) CUDA_TRY(cudaMalloc(&b->mem, devb + tab));
+    std::vector<Dev> devs(n);
+    for (uint32_t i = 0; i < n; ++i) devs[i] = b->sims[i]->d;
+    std::vector<uint32_t> t;
+    t.reserve(4 * n + 3);
+    t.insert(t.end(), demog_off.begin(), demog_off.end());
+    t.insert(t.end(), demog_h.begin(), demog_h.end());
+    t.insert(t.end(), foi_off.begin(), foi_off.end());
+    t.insert(t.end(), infect_off.begin(), infect_off.end());
+    CUDA_TRY(cudaMemcpy(b->mem, devs.data(), sizeof(Dev) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy((char*)b->mem + devb, t.data(), tab, cudaMemcpyHostToDevice));
+    uint32_t* tp = (uint32_t*)((char*)b->mem + devb);
+    BatchDev bd{};
+    bd.devs = (const Dev*)b->mem;
+    bd.demog_off = tp;
+    bd.demog_h = tp + (n + 1);
+    bd.foi_off = tp + (2 * n + 1);
+    bd.infect_off = tp + (3 * n + 2);
+    bd.n = n;
+    b->blocks[0] = demog_off[n];
+    b->blocks[1] = foi_off[n];
+    b->blocks[2] = infect_off[n];
+    bd.grid_demog = std::max(1u, std::min(b->blocks[0], l.numSM * occ[0]));
+    bd.grid_foi = std::max(1u, std::min(b->blocks[1], l.numSM * occ[1]));
+    bd.grid_infect = std::max(1u, std::min(b->blocks[2], l.numSM * occ[2]));
+    batch_drop_graphs(b);
+    b->bd = bd;
+    b->l = l;
+    b->arch = a;
+    return ARBO_OK;
+}
+
+int batch_ready(arbo_batch* b, uint32_t* t_out)
+{
+    uint32_t t = 0;
+    for (size_t i = 0; i < b->sims.size(); ++i) {
+        const arbo_sim* s = b->sims[i];
+        if (!s->inited) return fail(ARBO_ERR_STATE, "batch instance " + std::to_string(i) + " is not initialised");
+        if (i == 0) t = s->host_t;
+        else if (s->host_t != t)
+            return fail(ARBO_ERR_STATE, "batch instances are at different steps (step them through the batch only)");
+    }
+    *t_out = t;
+    return ARBO_OK;
+}
+
+// Steps that every instance can still take.
+uint32_t batch_room(const arbo_batch* b, uint32_t t)
+{
+    uint32_t room = UINT32_MAX;
+    for (const arbo_sim* s : b->sims) room = std::min(room, s->d.T - t);
+    return room;
+}
+
+void batch_advance_host(arbo_batch* b, uint32_t n)
+{
+    for (arbo_sim* s : b->sims) s->host_t += n;
+}
+
+int batch_capture(arbo_batch* b, uint32_t steps, cudaGraphExec_t* out)
+{
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t k = 0; k <= steps; ++k) {
+        const int e = k < steps ? launch_step_batch(b->bd, b->l, b->cap, nullptr, k)
+                                : launch_advance_batch(b->bd, steps, b->cap);
+        if (e) {
+            cudaStreamEndCapture(b->cap, &g);
+            if (g) cudaGraphDestroy(g);
+            return fail(ARBO_ERR_CUDA, std::string("batch step capture: ") + cudaGetErrorString((cudaError_t)e));
+        }
+    }
+    CUDA_TRY(cudaStreamEndCapture(b->cap, &g));
+    const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(ARBO_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+    return ARBO_OK;
+}
+
+int batch_flush(arbo_batch* b, uint32_t flush_mb, cudaStream_t st)
+{
+    if (!flush_mb) return ARBO_OK;
+    const size_t want = (size_t)flush_mb << 20;
+    if (b->flush_bytes < want) {
+        if (b->flush) cudaFree(b->flush);
+        b->flush = nullptr;
+        b->flush_bytes = 0;
+        CUDA_TRY(cudaMalloc(&b->flush, want + 256));
+        CUDA_TRY(cudaMemset(b->flush, 0, want + 256));
+        b->flush_bytes = want;
+    }
+    const int e = launch_l2_flush(b->flush, want, (uint32_t*)((char*)b->flush + b->flush_bytes), b->l.numSM, st);
+    return e ? fail(ARBO_ERR_CUDA, std::string("flush launch: ") + cudaGetErrorString((cudaError_t)e)) : ARBO_OK;
+}
+
+// Mean ms per phase over n directly launched steps: [demographic, force of infection, infection, step].
+int batch_phases(arbo_batch* b, uint32_t n, uint32_t flush_mb, cudaStream_t st, double acc[4])
+{
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.0;
+    for (uint32_t k = 0; k < n; ++k) {
+        int e = batch_flush(b, flush_mb, st);
+        if (e) return e;
+        e = launch_step_batch(b->bd, b->l, st, b->ev, 0);
+        if (!e) e = launch_advance_batch(b->bd, 1, st);
+        if (e) return fail(ARBO_ERR_CUDA, std::string("batch step launch: ") + cudaGetErrorString((cudaError_t)e));
+        batch_advance_host(b, 1);
+        CUDA_TRY(cudaEventSynchronize(b->ev[3]));
+        float x[4] = {0, 0, 0, 0};
+        CUDA_TRY(cudaEventElapsedTime(&x[0], b->ev[0], b->ev[1]));
+        CUDA_TRY(cudaEventElapsedTime(&x[1], b->ev[1], b->ev[2]));
+        CUDA_TRY(cudaEventElapsedTime(&x[2], b->ev[2], b->ev[3]));
+        CUDA_TRY(cudaEventElapsedTime(&x[3], b->ev[0], b->ev[3]));
+        for (int j = 0; j < 4; ++j) acc[j] += x[j];
+    }
+    for (int j = 0; j < 4; ++j) acc[j] = n ? acc[j] / n : 0.0;
+    return ARBO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int arbo_batch_create(arbo_sim* const* sims, uint32_t n, const arbo_arch_param* arch, arbo_batch** out)
+{
+    if (!sims || !out || n == 0) return fail(ARBO_ERR_INVALID, "arbo_batch_create: need at least one handle");
+    *out = nullptr;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!sims[i]) return fail(ARBO_ERR_INVALID, "arbo_batch_create: null handle " + std::to_string(i));
+        if (sims[i]->device != sims[0]->device)
+            return fail(ARBO_ERR_INVALID, "arbo_batch_create: all handles must live on one device");
+        for (uint32_t j = 0; j < i; ++j)
+            if (sims[j] == sims[i]) return fail(ARBO_ERR_INVALID, "arbo_batch_create: a handle appears twice");
+    }
+    arbo_batch* b = new arbo_batch();
+    b->sims.assign(sims, sims + n);
+    b->device = sims[0]->device;
+    auto bail = [&](int code) {
+        arbo_batch_destroy(b);
+        return code;
+    };
+    if (cudaSetDevice(b->device) != cudaSuccess) return bail(fail(ARBO_ERR_CUDA, "cudaSetDevice"));
+    if (cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(ARBO_ERR_CUDA, "cudaStreamCreate"));
+    for (int k = 0; k < 4; ++k)
+        if (cudaEventCreate(&b->ev[k]) != cudaSuccess) return bail(fail(ARBO_ERR_CUDA, "cudaEventCreate"));
+    const int e = batch_configure(b, arch ? *arch : sims[0]->arch);
+    if (e) return bail(e);
+    *out = b;
+    return ARBO_OK;
+}
+
+int arbo_batch_destroy(arbo_batch* b)
+{
+    if (!b) return ARBO_OK;
+    cudaSetDevice(b->device);
+    batch_drop_graphs(b);
+    for (int k = 0; k < 4; ++k)
+        if (b->ev[k]) cudaEventDestroy(b->ev[k]);
+    for (cudaEvent_t e : b->step_ev) cudaEventDestroy(e);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->flush) cudaFree(b->flush);
+    if (b->mem) cudaFree(b->mem);
+    delete b;
+    return ARBO_OK;
+}
+
+int arbo_batch_size(const arbo_batch* b, uint32_t* n, uint64_t* agents)
+{
+    if (!b) return fail(ARBO_ERR_INVALID, "null batch");
+    uint64_t a = 0;
+    for (const arbo_sim* s : b->sims) a += (uint64_t)s->d.N + s->d.M;
+    if (n) *n = (uint32_t)b->sims.size();
+    if (agents) *agents = a;
+    return ARBO_OK;
+}
+
+int arbo_batch_set_arch(arbo_batch* b, const arbo_arch_param* arch)
+{
+    if (!b || !arch) return fail(ARBO_ERR_INVALID, "null argument");
+    CUDA_TRY(cudaSetDevice(b->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // graphs of the old shape may still run
+    return batch_configure(b, *arch);
+}
+
+int arbo_batch_get_arch(const arbo_batch* b, arbo_arch_param* arch, uint32_t grids[3])
+{
+    if (!b || !arch) return fail(ARBO_ERR_INVALID, "null argument");
+    *arch = b->arch;
+    if (grids) {
+        grids[0] = b->bd.grid_demog;
+        grids[1] = b->bd.grid_foi;
+        grids[2] = b->bd.grid_infect;
+    }
+    return ARBO_OK;
+}
+
+int arbo_batch_init(arbo_batch* b, void* stream)
+{
+    if (!b) return fail(ARBO_ERR_INVALID, "null batch");
+    for (arbo_sim* s : b->sims) {
+        const int e = arbo_sim_init(s, stream);
+        if (e) return e;
+    }
+    return ARBO_OK;
+}
+
+int arbo_batch_step(arbo_batch* b, uint32_t nsteps, void* stream)
+{
+    if (!b) return fail(ARBO_ERR_INVALID, "null batch");
+    uint32_t t = 0;
+    int e = batch_ready(b, &t);
+    if (e) return e;
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t n = std::min(nsteps, batch_room(b, t));
+    const uint32_t G = b->arch.graphSteps;
+    if (G == 0) {
+        for (uint32_t k = 0; k < n; ++k) {
+            e = launch_step_batch(b->bd, b->l, st, nullptr, 0);
+            if (!e) e = launch_advance_batch(b->bd, 1, st);
+            if (e) return fail(ARBO_ERR_CUDA, std::string("batch step launch: ") + cudaGetErrorString((cudaError_t)e));
+            batch_advance_host(b, 1);
+        }
+        return ARBO_OK;
+    }
+    if (n >= G && !b->gmulti && (e = batch_capture(b, G, &b->gmulti))) return e;
+    while (n >= G) {
+        CUDA_TRY(cudaGraphLaunch(b->gmulti, st));
+        n -= G;
+        batch_advance_host(b, G);
+    }
+    if (n > 0 && !b->gone && (e = batch_capture(b, 1, &b->gone))) return e;
+    while (n > 0) {
+        CUDA_TRY(cudaGraphLaunch(b->gone, st));
+        n -= 1;
+        batch_advance_host(b, 1);
+    }
+    return ARBO_OK;
+}
+
+int arbo_batch_run(arbo_batch* b, void* stream)
+{
+    return arbo_batch_step(b, UINT32_MAX, stream);
+}
+
+int arbo_batch_time_phases(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* ms_out, void* stream)
+{
+    if (!b || !ms_out) return fail(ARBO_ERR_INVALID, "null argument");
+    uint32_t t = 0;
+    int e = batch_ready(b, &t);
+    if (e) return e;
+    CUDA_TRY(cudaSetDevice(b->device));
+    double acc[4];
+    if ((e = batch_phases(b, std::min(nsteps, batch_room(b, t)), flush_mb, (cudaStream_t)stream, acc))) return e;
+    for (int j = 0; j < 4; ++j) ms_out[j] = (float)acc[j];
+    return ARBO_OK;
+}
+
+int arbo_batch_time_steps(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* step_ms, void* stream)
+{
+    if (!b || !step_ms) return fail(ARBO_ERR_INVALID, "null argument");
+    uint32_t t = 0;
+    int e = batch_ready(b, &t);
+    if (e) return e;
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t n = std::min(nsteps, batch_room(b, t));
+    for (uint32_t k = n; k < nsteps; ++k) step_ms[k] = 0.0f;
+    while (b->step_ev.size() < 2) {
+        cudaEvent_t ev;
+        CUDA_TRY(cudaEventCreate(&ev));
+        b->step_ev.push_back(ev);
+    }
+    // One graph-launched step at a time, each between its own events (optional L2 flush first).
+    cudaGraphExec_t one = nullptr;
+    if ((e = batch_capture(b, 1, &one))) return e;
+    for (uint32_t k = 0; k < n; ++k) {
+        if ((e = batch_flush(b, flush_mb, st))) break;
+        cudaError_t ce = cudaEventRecord(b->step_ev[0], st);
+        if (ce == cudaSuccess) ce = cudaGraphLaunch(one, st);
+        if (ce == cudaSuccess) ce = cudaEventRecord(b->step_ev[1], st);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(b->step_ev[1]);
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&step_ms[k], b->step_ev[0], b->step_ev[1]);
+        if (ce != cudaSuccess) {
+            e = fail(ARBO_ERR_CUDA, std::string("timed batch steps: ") + cudaGetErrorString(ce));
+            break;
+        }
+        batch_advance_host(b, 1);
+    }
+    cudaGraphExecDestroy(one);
+    return e;
+}
+
+int arbo_batch_autotune(arbo_batch* b, uint32_t steps_per_candidate, arbo_arch_param* best, float* best_ms,
+                        void* stream)
+{
+    if (!b || steps_per_candidate == 0) return fail(ARBO_ERR_INVALID, "arbo_batch_autotune: bad arguments");
+    uint32_t t = 0;
+    int e = batch_ready(b, &t);
+    if (e) return e;
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    static const uint32_t demog[][2] = {{256, 2}, {256, 1}, {128, 2}, {128, 1}, {256, 4}, {64, 1}};
+    static const uint32_t foi[] = {256, 128, 512};
+    static const uint32_t infect[] = {256, 128, 512, 64};
+    const uint32_t need = steps_per_candidate * (uint32_t)(6 + 3 + 4);
+    if (batch_room(b, t) < need)
+        return fail(ARBO_ERR_STATE, "arbo_batch_autotune: " + std::to_string(need) + " steps needed, " +
+                                        std::to_string(batch_room(b, t)) + " left");
+    // Coordinate search: every candidate runs real steps (results do not depend on the launch
+    // shape), each phase keeps the shape with the smallest mean time.
+    arbo_arch_param cur = b->arch;
+    double acc[4];
+    double bd = 1e30, bf = 1e30, bi = 1e30;
+    arbo_arch_param pick = cur;
+    for (const auto& c : demog) {
+        arbo_arch_param a = cur;
+        a.demogBlock = c[0];
+        a.demogUnroll = c[1];
+        if ((e = batch_configure(b, a)) || (e = batch_phases(b, steps_per_candidate, 0, st, acc))) return e;
+        if (acc[0] < bd) {
+            bd = acc[0];
+            pick.demogBlock = c[0];
+            pick.demogUnroll = c[1];
+        }
+    }
+    for (uint32_t f : foi) {
+        arbo_arch_param a = pick;
+        a.foiBlock = f;
+        if ((e = batch_configure(b, a)) || (e = batch_phases(b, steps_per_candidate, 0, st, acc))) return e;
+        if (acc[1] < bf) {
+            bf = acc[1];
+            pick.foiBlock = f;
+        }
+    }
+    for (uint32_t f : infect) {
+        arbo_arch_param a = pick;
+        a.infectBlock = f;
+        if ((e = batch_configure(b, a)) || (e = batch_phases(b, steps_per_candidate, 0, st, acc))) return e;
+        if (acc[2] < bi) {
+            bi = acc[2];
+            pick.infectBlock = f;
+        }
+    }
+    if ((e = batch_configure(b, pick))) return e;
+    if (best) *best = pick;
+    if (best_ms) {
+        best_ms[0] = (float)bd;
+        best_ms[1] = (float)bf;
+        best_ms[2] = (float)bi;
+    }
+    return ARBO_OK;
+}
+
+}  // extern "C"

@@ -210,7 +210,6 @@ __device__ __noinline__ void mosq_counter(uint32_t* infm, const uint8_t* m_strai
     if (add > 0) atomicAdd(p, 1u); else counter_dec(p, ctrl);
 }
 
-constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 
 // Bit 7 of each byte of x gathered into a 4-bit mask (byte k -> bit k).
 __device__ __forceinline__ uint32_t nibble7(uint32_t x)
@@ -583,20 +582,28 @@ __global__ void __launch_bounds__(128, 4) k_demog_tma(Dev d, uint32_t koff)
     griddep_launch_dependents();
 }
 
+// Block b of the demographic pass of one simulation: blocks below hblocks age humans, the others
+// run one mosquito quad per warp.
+template <int U>
+__device__ __forceinline__ void demog_block(const Dev& d, uint32_t b, uint32_t hblocks, uint32_t koff, QuadSmem* wsm)
+{
+    const uint32_t t = d.ctrl->t + koff;
+    const Key key = load_key(d.ctrl);
+    if (b < hblocks) {
+        demog_humans<U>(d, key, b * blockDim.x * U + threadIdx.x, blockDim.x, t);
+    } else {
+        const uint32_t wpb = blockDim.x >> 5;
+        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+        const uint32_t q = (b - hblocks) * wpb + warp;
+        if (q * kQuad < d.tiles) demog_mosquito_quad(d, key, q, lane, t, wsm[warp]);
+    }
+}
+
 template <int U>
 __global__ void __launch_bounds__(256, 4) k_demog(Dev d, uint32_t hblocks, uint32_t koff)
 {
     __shared__ QuadSmem wsm[8];
-    const uint32_t t = d.ctrl->t + koff;
-    const Key key = load_key(d.ctrl);
-    if (blockIdx.x < hblocks) {
-        demog_humans<U>(d, key, blockIdx.x * blockDim.x * U + threadIdx.x, blockDim.x, t);
-    } else {
-        const uint32_t wpb = blockDim.x >> 5;
-        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-        const uint32_t q = (blockIdx.x - hblocks) * wpb + warp;
-        if (q * kQuad < d.tiles) demog_mosquito_quad(d, key, q, lane, t, wsm[warp]);
-    }
+    demog_block<U>(d, blockIdx.x, hblocks, koff, wsm);
     griddep_launch_dependents();
 }
 
@@ -630,18 +637,27 @@ __device__ __forceinline__ void split_events(const Dev& d, uint32_t* trans, floa
 // Series row + force of infection. A CTA of 4*K threads owns K consecutive (serotype,
 // community) pairs: K threads read the counters, add the series sums and split each pair's
 // events; then all threads spread the flattened events of the K pairs, four per Philox call.
-__global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t koff)
+struct FoiSmem {
+    uint32_t cnt[512], scan[513], loc[128], deg[128], sum[3 * ARBO_MAX_STRAINS + 2], wt[16];
+    uint32_t to[128][8];  // CSR row of each pair's source community (degree <= 8)
+};
+
+__device__ __forceinline__ void foi_block(const Dev& d, uint32_t b, int collect_only, uint32_t koff, FoiSmem& fs)
 {
-    __shared__ uint32_t s_cnt[512], s_scan[513], s_loc[128], s_deg[128], s_sum[3 * ARBO_MAX_STRAINS + 2],
-        s_wt[16];
-    __shared__ uint32_t s_to[128][8];  // CSR row of each pair's source community (degree <= 8)
+    uint32_t* const s_cnt = fs.cnt;
+    uint32_t* const s_scan = fs.scan;
+    uint32_t* const s_loc = fs.loc;
+    uint32_t* const s_deg = fs.deg;
+    uint32_t* const s_sum = fs.sum;
+    uint32_t* const s_wt = fs.wt;
+    uint32_t(*const s_to)[8] = fs.to;
     const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
     const uint32_t row = collect_only ? 0u : t + 1;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t K = blockDim.x >> 2;
     const uint32_t SP = d.S * d.P, S = d.S, P = d.P;
-    const uint32_t p0 = blockIdx.x * K;
+    const uint32_t p0 = b * K;
     if (tid < 3 * ARBO_MAX_STRAINS + 2) s_sum[tid] = 0;
     __syncthreads();
     uint32_t nk[4] = {0, 0, 0, 0};
@@ -757,6 +773,12 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
     }
 }
 
+__global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t koff)
+{
+    __shared__ FoiSmem fs;
+    foi_block(d, blockIdx.x, collect_only, koff, fs);
+}
+
 // ------------------------------------------------------------------ infection draws
 
 __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r)
@@ -842,9 +864,9 @@ __device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, ui
 //   C: each event that won its target applies its infection.
 // This reproduces the serial loops of nmTransmission / mnTransmission (cpp/mepidemic.cu:143-246,
 // cpp/nepidemic.cu:146-319): a target is infected by the first eligible event in serial order.
-__global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
+// Communities cb..cb+K-1 of one simulation (K = blockDim.x / 64, at least 1).
+__device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t koff, InfectSmem& sh)
 {
-    __shared__ InfectSmem sh;
     const uint32_t t = d.ctrl->t + koff;
     const uint32_t epoch = d.ctrl->epoch + koff;
     const uint32_t hiword = ~epoch;
@@ -853,190 +875,265 @@ __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
     const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
     const uint32_t S = d.S, P = d.P;
     const float ext = __fdiv_rn(d.extInf, (float)P);
-
-    for (uint32_t cb = blockIdx.x * K; cb < P; cb += gridDim.x * K) {
-        const uint32_t c = cb + warp;
-        const bool owner = warp < K && c < P;
-        uint32_t ne = 0;
-        uint32_t items = 0;
-        if (owner) {
-            // Static loads and keyed draws first; the event counts and alive mosquitoes written by
-            // the previous kernels are read after the programmatic-launch wait.
-            const uint32_t ns = __ldg(&d.nsize[c]);
-            const uint32_t ms = __ldg(&d.msize[c]);
-            const uint32_t nb0 = __ldg(&d.nloc[c]), mb0 = __ldg(&d.mloc[c]);
-            const uint32_t pl = lane * P + c;
-            U4 rd;
-            if (lane < S) rd = draw4(key, kIntroCount, pl, t);
-            else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
-            else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
-            griddep_wait();
-            const uint32_t mc = d.mcnt[c];
-            uint32_t kh = lane < S ? d.transh[pl] : 0u;
-            uint32_t km = lane < S ? d.transm[pl] : 0u;
-            uint32_t sv = 0;
-            if (lane < S) {
-                if (kh) d.transh[pl] = 0;
-                if (km) d.transm[pl] = 0;
-                if (ns == 0) kh = 0;
-                else ne = (uint32_t)resolve(ext, rd.v[0]);
-                if (mc == 0) km = 0;
-                if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
-                    atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
-                    kh = min(kh, kMaxEventsPerPair - 1);
-                    km = min(km, kMaxEventsPerPair - 1);
-                }
-            } else if (lane == 8) {
-                if (mc) sv = bounded(rd.v[0], S);
-            } else if (lane == 9) {
-                if (ns) sv = bounded(rd.v[0], S);
-            }
-            const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
-            uint32_t H = 0, Mt = 0;
-            for (uint32_t j = 0; j < S; ++j) {
-                const uint32_t khj = __shfl_sync(kFull, kh, (s0h + j) % S);
-                const uint32_t kmj = __shfl_sync(kFull, km, (s0m + j) % S);
-                if (lane == 0) {
-                    sh.hstart[warp][j] = H;
-                    sh.mstart[warp][j] = Mt;
-                    sh.kh[warp][j] = khj;
-                    sh.km[warp][j] = kmj;
-                }
-                H += (khj + 3) >> 2;
-                Mt += kmj;
-            }
-            if (lane == 0) {
-                sh.hitems[warp] = H;
-                sh.c[warp] = c;
-                sh.s0h[warp] = s0h;
-                sh.s0m[warp] = s0m;
-                sh.nbase[warp] = nb0;
-                sh.mbase[warp] = mb0;
-                sh.ns[warp] = ns;
-                sh.ms[warp] = ms;
-            }
-            items = H + Mt;
-        }
+    const uint32_t c = cb + warp;
+    const bool owner = warp < K && c < P;
+    uint32_t ne = 0;
+    uint32_t items = 0;
+    if (owner) {
+        // Static loads and keyed draws first; the event counts and alive mosquitoes written by
+        // the previous kernels are read after the programmatic-launch wait.
+        const uint32_t ns = __ldg(&d.nsize[c]);
+        const uint32_t ms = __ldg(&d.msize[c]);
+        const uint32_t nb0 = __ldg(&d.nloc[c]), mb0 = __ldg(&d.mloc[c]);
+        const uint32_t pl = lane * P + c;
+        U4 rd;
+        if (lane < S) rd = draw4(key, kIntroCount, pl, t);
+        else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
+        else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
         griddep_wait();
-        // Item starts of the K communities (serial over at most 8 entries).
-        if (lane == 0 && warp < K) sh.cstart[warp + 1] = items;
-        __syncthreads();
-        if (tid == 0) {
-            sh.cstart[0] = 0;
-            for (uint32_t w = 1; w <= K; ++w) sh.cstart[w] += sh.cstart[w - 1];
+        const uint32_t mc = d.mcnt[c];
+        uint32_t kh = lane < S ? d.transh[pl] : 0u;
+        uint32_t km = lane < S ? d.transm[pl] : 0u;
+        uint32_t sv = 0;
+        if (lane < S) {
+            if (kh) d.transh[pl] = 0;
+            if (km) d.transm[pl] = 0;
+            if (ns == 0) kh = 0;
+            else ne = (uint32_t)resolve(ext, rd.v[0]);
+            if (mc == 0) km = 0;
+            if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
+                atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
+                kh = min(kh, kMaxEventsPerPair - 1);
+                km = min(km, kMaxEventsPerPair - 1);
+            }
+        } else if (lane == 8) {
+            if (mc) sv = bounded(rd.v[0], S);
+        } else if (lane == 9) {
+            if (ns) sv = bounded(rd.v[0], S);
         }
-        __syncthreads();
-        const uint32_t total = sh.cstart[K];
-        const uint32_t any_intro = __syncthreads_or(ne != 0);
-        if (total == 0 && !any_intro) continue;
+        const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
+        uint32_t H = 0, Mt = 0;
+        for (uint32_t j = 0; j < S; ++j) {
+            const uint32_t khj = __shfl_sync(kFull, kh, (s0h + j) % S);
+            const uint32_t kmj = __shfl_sync(kFull, km, (s0m + j) % S);
+            if (lane == 0) {
+                sh.hstart[warp][j] = H;
+                sh.mstart[warp][j] = Mt;
+                sh.kh[warp][j] = khj;
+                sh.km[warp][j] = kmj;
+            }
+            H += (khj + 3) >> 2;
+            Mt += kmj;
+        }
+        if (lane == 0) {
+            sh.hitems[warp] = H;
+            sh.c[warp] = c;
+            sh.s0h[warp] = s0h;
+            sh.s0m[warp] = s0m;
+            sh.nbase[warp] = nb0;
+            sh.mbase[warp] = mb0;
+            sh.ns[warp] = ns;
+            sh.ms[warp] = ms;
+        }
+        items = H + Mt;
+    }
+    griddep_wait();
+    // Item starts of the K communities (serial over at most 8 entries).
+    if (lane == 0 && warp < K) sh.cstart[warp + 1] = items;
+    __syncthreads();
+    if (tid == 0) {
+        sh.cstart[0] = 0;
+        for (uint32_t w = 1; w <= K; ++w) sh.cstart[w] += sh.cstart[w - 1];
+    }
+    __syncthreads();
+    const uint32_t total = sh.cstart[K];
+    const uint32_t any_intro = __syncthreads_or(ne != 0);
+    if (total == 0 && !any_intro) return;
 
-        // Phase A
-        for (uint32_t it = tid; it < total; it += blockDim.x) {
-            uint32_t w, j, idx;
-            bool human;
-            decode_item(sh, K, S, it, &w, &j, &human, &idx);
-            const uint32_t cc = sh.c[w];
-            if (human) {
-                const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+    // Phase A
+    for (uint32_t it = tid; it < total; it += blockDim.x) {
+        uint32_t w, j, idx;
+        bool human;
+        decode_item(sh, K, S, it, &w, &j, &human, &idx);
+        const uint32_t cc = sh.c[w];
+        if (human) {
+            const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+            const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+            uint32_t tg[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+            if (it < kTargetCache) sh.target[it] = make_uint4(tg[0], tg[1], tg[2], tg[3]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t e = 4 * idx + q;
+                if (e >= k) break;
+                const uint32_t st = d.n_status[tg[q]], im = d.n_imm[tg[q]];
+                if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[tg[q]], order_key(hiword, j, 0, e));
+            }
+        } else {
+            const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+            const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+            if (it < kTargetCache) sh.target[it].x = slot;
+            if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
+            else if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
+        }
+    }
+    __syncthreads();
+    // Phase B: warp w handles the introductions of its own community.
+    if (any_intro && owner) {
+        const uint32_t s0h = sh.s0h[warp], nbase = sh.nbase[warp], ns = sh.ns[warp];
+        for (uint32_t j = 0; j < S; ++j) {
+            const uint32_t s = (s0h + j) % S, ph = s * P + c;
+            uint32_t left = __shfl_sync(kFull, ne, s);
+            if (left == 0) continue;
+            uint32_t a0 = 0;
+            while (left > 0 && a0 < d.maxIntro) {
+                const uint32_t a = a0 + lane;
+                bool elig = false;
+                uint32_t i = 0;
+                unsigned long long okey = 0;
+                if (a < d.maxIntro) {
+                    const U4 r = draw4(key, kIntroTarget, ph, t, a >> 2);
+                    i = nbase + bounded(r.v[a & 3], ns);
+                    okey = order_key(hiword, j, 1, a);
+                    elig = __ldcg(&d.n_status[i]) == 0 && !((__ldcg(&d.n_imm[i]) >> s) & 1u) &&
+                           __ldcg(&d.winh[i]) > okey;
+                }
+                const unsigned bal = __ballot_sync(kFull, elig);
+                if (!bal) {
+                    a0 += 32;
+                    continue;
+                }
+                const uint32_t pl = __ffs(bal) - 1;
+                if (lane == pl) {
+                    d.winh[i] = okey;
+                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a));
+                }
+                __syncwarp();
+                left -= 1;
+                a0 = a0 + pl + 1;
+            }
+            if (left > 0 && lane == 0) atomicAdd(&d.ctrl->diag[1], 1u);
+        }
+    }
+    __syncthreads();
+    // Phase C
+    for (uint32_t it = tid; it < total; it += blockDim.x) {
+        uint32_t w, j, idx;
+        bool human;
+        decode_item(sh, K, S, it, &w, &j, &human, &idx);
+        const uint32_t cc = sh.c[w];
+        if (human) {
+            const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+            uint32_t tg[4];
+            if (it < kTargetCache) {
+                const uint4 v = sh.target[it];
+                tg[0] = v.x;
+                tg[1] = v.y;
+                tg[2] = v.z;
+                tg[3] = v.w;
+            } else {
                 const U4 r = draw4(key, kInfHTarget, ph, t, idx);
-                uint32_t tg[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
-                if (it < kTargetCache) sh.target[it] = make_uint4(tg[0], tg[1], tg[2], tg[3]);
+            }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t e = 4 * idx + q;
-                    if (e >= k) break;
-                    const uint32_t st = d.n_status[tg[q]], im = d.n_imm[tg[q]];
-                    if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[tg[q]], order_key(hiword, j, 0, e));
-                }
-            } else {
-                const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
-                const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
-                if (it < kTargetCache) sh.target[it].x = slot;
-                if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
-                else if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t e = 4 * idx + q;
+                if (e >= k) break;
+                if (__ldcg(&d.winh[tg[q]]) == order_key(hiword, j, 0, e))
+                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e));
+            }
+        } else {
+            const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+            const uint32_t slot = it < kTargetCache ? sh.target[it].x
+                                                    : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+            if (slot != UINT_MAX && __ldcg(&d.winm[slot]) == order_key(hiword, j, 0, idx)) {
+                const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
+                d.m_state[slot] = 1;
+                d.m_strain[slot] = (uint8_t)sm;
+                d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)d.m_age[slot], d.mExposed), r.v[idx & 3]);
             }
         }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
+{
+    __shared__ InfectSmem sh;
+    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
+    for (uint32_t cb = blockIdx.x * K; cb < d.P; cb += gridDim.x * K) infect_block(d, cb, koff, sh);
+}
+
+// ------------------------------------------------------------------ batched steps
+
+// Instance owning flattened block b: the largest i with off[i] <= b.
+__device__ __forceinline__ uint32_t batch_instance(const uint32_t* __restrict__ off, uint32_t n, uint32_t b)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(&off[mid]) <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Block-uniform walk over the flattened blocks of a phase. For every block the descriptor of its
+// instance is staged into shared memory (only when the instance changes) and fn(dev, inst, b) runs.
+template <typename Fn>
+__device__ __forceinline__ void batch_loop(const BatchDev& bd, const uint32_t* __restrict__ off, Fn fn)
+{
+    __shared__ __align__(16) unsigned long long raw[sizeof(Dev) / 8];
+    __shared__ uint32_t s_inst;
+    const Dev& d = *reinterpret_cast<const Dev*>(raw);
+    const uint32_t total = __ldg(&off[bd.n]);
+    uint32_t cur = UINT_MAX;
+    for (uint32_t b = blockIdx.x; b < total; b += gridDim.x) {
+        __syncthreads();  // the previous block's readers of raw / s_inst are done
+        if (threadIdx.x == 0) s_inst = batch_instance(off, bd.n, b);
         __syncthreads();
-        // Phase B: warp w handles the introductions of its own community.
-        if (any_intro && owner) {
-            const uint32_t s0h = sh.s0h[warp], nbase = sh.nbase[warp], ns = sh.ns[warp];
-            for (uint32_t j = 0; j < S; ++j) {
-                const uint32_t s = (s0h + j) % S, ph = s * P + c;
-                uint32_t left = __shfl_sync(kFull, ne, s);
-                if (left == 0) continue;
-                uint32_t a0 = 0;
-                while (left > 0 && a0 < d.maxIntro) {
-                    const uint32_t a = a0 + lane;
-                    bool elig = false;
-                    uint32_t i = 0;
-                    unsigned long long okey = 0;
-                    if (a < d.maxIntro) {
-                        const U4 r = draw4(key, kIntroTarget, ph, t, a >> 2);
-                        i = nbase + bounded(r.v[a & 3], ns);
-                        okey = order_key(hiword, j, 1, a);
-                        elig = __ldcg(&d.n_status[i]) == 0 && !((__ldcg(&d.n_imm[i]) >> s) & 1u) &&
-                               __ldcg(&d.winh[i]) > okey;
-                    }
-                    const unsigned bal = __ballot_sync(kFull, elig);
-                    if (!bal) {
-                        a0 += 32;
-                        continue;
-                    }
-                    const uint32_t pl = __ffs(bal) - 1;
-                    if (lane == pl) {
-                        d.winh[i] = okey;
-                        infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a));
-                    }
-                    __syncwarp();
-                    left -= 1;
-                    a0 = a0 + pl + 1;
-                }
-                if (left > 0 && lane == 0) atomicAdd(&d.ctrl->diag[1], 1u);
-            }
+        const uint32_t inst = s_inst;
+        if (inst != cur) {
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
+            for (uint32_t i = threadIdx.x; i < sizeof(Dev) / 8; i += blockDim.x) raw[i] = src[i];
+            cur = inst;
+            __syncthreads();
         }
-        __syncthreads();
-        // Phase C
-        for (uint32_t it = tid; it < total; it += blockDim.x) {
-            uint32_t w, j, idx;
-            bool human;
-            decode_item(sh, K, S, it, &w, &j, &human, &idx);
-            const uint32_t cc = sh.c[w];
-            if (human) {
-                const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
-                uint32_t tg[4];
-                if (it < kTargetCache) {
-                    const uint4 v = sh.target[it];
-                    tg[0] = v.x;
-                    tg[1] = v.y;
-                    tg[2] = v.z;
-                    tg[3] = v.w;
-                } else {
-                    const U4 r = draw4(key, kInfHTarget, ph, t, idx);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t e = 4 * idx + q;
-                    if (e >= k) break;
-                    if (__ldcg(&d.winh[tg[q]]) == order_key(hiword, j, 0, e))
-                        infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e));
-                }
-            } else {
-                const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
-                const uint32_t slot = it < kTargetCache ? sh.target[it].x
-                                                        : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
-                if (slot != UINT_MAX && __ldcg(&d.winm[slot]) == order_key(hiword, j, 0, idx)) {
-                    const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
-                    d.m_state[slot] = 1;
-                    d.m_strain[slot] = (uint8_t)sm;
-                    d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)d.m_age[slot], d.mExposed), r.v[idx & 3]);
-                }
-            }
-        }
-        __syncthreads();
+        fn(d, inst, b - __ldg(&off[inst]));
+    }
+}
+
+template <int U>
+__global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t koff)
+{
+    __shared__ QuadSmem wsm[8];
+    batch_loop(bd, bd.demog_off, [&](const Dev& d, uint32_t inst, uint32_t b) {
+        demog_block<U>(d, b, __ldg(&bd.demog_h[inst]), koff, wsm);
+    });
+    griddep_launch_dependents();
+}
+
+__global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
+{
+    __shared__ FoiSmem fs;
+    batch_loop(bd, bd.foi_off, [&](const Dev& d, uint32_t, uint32_t b) { foi_block(d, b, 0, koff, fs); });
+}
+
+__global__ void __launch_bounds__(512) k_infect_batch(BatchDev bd, uint32_t koff)
+{
+    __shared__ InfectSmem sh;
+    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
+    batch_loop(bd, bd.infect_off, [&](const Dev& d, uint32_t, uint32_t b) { infect_block(d, b * K, koff, sh); });
+}
+
+__global__ void k_advance_batch(BatchDev bd, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < bd.n) {
+        Ctrl* c = bd.devs[i].ctrl;
+        c->t += n;
+        c->epoch += n;
     }
 }
 
@@ -1167,7 +1264,6 @@ __global__ void k_seed(Dev d)
     }
 }
 
-inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 // Reads a buffer larger than L2 so that the next kernel starts with a cold cache. The loads
 // feed a comparison that never holds for the zero-filled buffer, so they cannot be elided.
@@ -1311,5 +1407,48 @@ int launch_advance(const Dev& d, uint32_t n, void* stream)
 }
 
 uint32_t launches_per_step() { return 3; }
+
+int batch_blocks_per_sm(const Launch& l, uint32_t out[3])
+{
+    int n = 0;
+    cudaError_t e;
+    if (l.demogUnroll == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_batch<4>, (int)l.demogBlock, 0);
+    else if (l.demogUnroll == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_batch<2>, (int)l.demogBlock, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_batch<1>, (int)l.demogBlock, 0);
+    if (e != cudaSuccess) return (int)e;
+    out[0] = n > 0 ? (uint32_t)n : 1u;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_foi_batch, (int)l.foiBlock, 0)) != cudaSuccess) return (int)e;
+    out[1] = n > 0 ? (uint32_t)n : 1u;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_infect_batch, (int)l.infectBlock, 0)) != cudaSuccess)
+        return (int)e;
+    out[2] = n > 0 ? (uint32_t)n : 1u;
+    return 0;
+}
+
+int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* events, uint32_t koff)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t* ev = (cudaEvent_t*)events;
+    int e;
+    if (ev) cudaEventRecord(ev[0], st);
+    const dim3 gd(bd.grid_demog), bdm(l.demogBlock);
+    if (l.demogUnroll == 4) k_demog_batch<4><<<gd, bdm, 0, st>>>(bd, koff);
+    else if (l.demogUnroll == 2) k_demog_batch<2><<<gd, bdm, 0, st>>>(bd, koff);
+    else k_demog_batch<1><<<gd, bdm, 0, st>>>(bd, koff);
+    if ((e = (int)cudaGetLastError())) return e;
+    if (ev) cudaEventRecord(ev[1], st);
+    if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), st, l.pdl != 0, bd, koff))) return e;
+    if (ev) cudaEventRecord(ev[2], st);
+    if ((e = launch_pdl(k_infect_batch, dim3(bd.grid_infect), dim3(l.infectBlock), st, l.pdl != 0, bd, koff)))
+        return e;
+    if (ev) cudaEventRecord(ev[3], st);
+    return 0;
+}
+
+int launch_advance_batch(const BatchDev& bd, uint32_t n, void* stream)
+{
+    k_advance_batch<<<cdiv(bd.n, 128), 128, 0, (cudaStream_t)stream>>>(bd, n);
+    return (int)cudaGetLastError();
+}
 
 }  // namespace arbo

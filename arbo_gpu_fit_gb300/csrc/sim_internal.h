@@ -24,6 +24,9 @@ namespace arbo {
 
 constexpr uint8_t kPad = 0xFF;        // status byte of a padding agent
 constexpr uint8_t kDead = 0x80;       // mosquito state: dead flag
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
 constexpr uint32_t kMaxEventsPerPair = 1u << 24;
 
@@ -101,6 +104,20 @@ struct Dev {
     Ctrl* ctrl;
 };
 
+static_assert(sizeof(Dev) % 16 == 0 || sizeof(Dev) % 8 == 0, "Dev is staged into shared memory in 8-byte words");
+
+// Many simulations stepped together (one persistent kernel per phase). The work of each phase is
+// the concatenation of the instances' blocks; off arrays hold each instance's first block.
+struct BatchDev {
+    const Dev* devs;             // [n] descriptors in device memory
+    const uint32_t* demog_off;   // [n+1] demographic blocks
+    const uint32_t* demog_h;     // [n] human blocks of each instance (the rest are mosquito blocks)
+    const uint32_t* foi_off;     // [n+1] force-of-infection blocks
+    const uint32_t* infect_off;  // [n+1] infection blocks (K communities each)
+    uint32_t n;
+    uint32_t grid_demog, grid_foi, grid_infect;  // resident CTAs of each persistent kernel
+};
+
 struct Launch {
     uint32_t demogBlock, demogUnroll, foiBlock, infectBlock, numSM, demogBlocksPerSM;
     uint32_t pdl;  // 1: k_foi and k_infect use programmatic dependent launch
@@ -119,6 +136,12 @@ int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint3
 // Adds n to the step counter and the winner epoch (one thread).
 int launch_advance(const Dev& d, uint32_t n, void* stream);
 uint32_t launches_per_step();
+
+// Batched steps (see BatchDev); the block shapes come from l, the grids from bd.
+int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* events, uint32_t koff);
+int launch_advance_batch(const BatchDev& bd, uint32_t n, void* stream);
+// Resident CTAs per SM of the three batched kernels for the block shapes of l.
+int batch_blocks_per_sm(const Launch& l, uint32_t out[3]);
 // Reads `bytes` of buf (a multiple of 16) to evict L2; `sink` is a device word never written in practice.
 int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_sm, cudaStream_t st);
 

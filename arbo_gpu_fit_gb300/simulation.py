@@ -277,6 +277,81 @@ class Simulation:
         return out
 
 
+class Batch:
+    """Many Simulation handles stepped together (arbo_batch_* of include/arbo.h): one persistent
+    kernel per phase over the blocks of every instance, the step loop in a CUDA graph. Each
+    instance's results equal stepping it alone; read them through the Simulation objects, which
+    must outlive the batch and be stepped only through it."""
+
+    def __init__(self, sims, arch: Optional[ArchitectureParam] = None, stream: int = 0):
+        self._lib = load()
+        self.sims = list(sims)
+        if not self.sims:
+            raise ValueError("a batch needs at least one simulation")
+        self.stream = c_void_p(stream or None)
+        hs = (c_void_p * len(self.sims))(*[s._h.value for s in self.sims])
+        h = c_void_p()
+        check(self._lib.arbo_batch_create(hs, len(self.sims), byref(arch) if arch is not None else None, byref(h)))
+        self._h = h
+        n, agents = c_uint32(), ctypes.c_uint64()
+        check(self._lib.arbo_batch_size(h, byref(n), byref(agents)))
+        self.n, self.agents = n.value, agents.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.arbo_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def init(self) -> None:
+        check(self._lib.arbo_batch_init(self._h, self.stream))
+
+    def step(self, nsteps: int = 1) -> None:
+        check(self._lib.arbo_batch_step(self._h, int(nsteps), self.stream))
+
+    def run(self) -> None:
+        check(self._lib.arbo_batch_run(self._h, self.stream))
+
+    def arch(self):
+        a = ArchitectureParam.__new__(ArchitectureParam)
+        ArchParamStruct.__init__(a)
+        grids = (c_uint32 * 3)()
+        check(self._lib.arbo_batch_get_arch(self._h, byref(a), grids))
+        return a, list(grids)
+
+    def set_arch(self, arch: ArchitectureParam) -> None:
+        check(self._lib.arbo_batch_set_arch(self._h, byref(arch)))
+
+    def autotune(self, steps_per_candidate: int = 2):
+        """Picks the launch shapes (coordinate search over real steps); returns (arch, phase ms)."""
+        a = ArchitectureParam.__new__(ArchitectureParam)
+        ArchParamStruct.__init__(a)
+        ms = (c_float * 3)()
+        check(self._lib.arbo_batch_autotune(self._h, int(steps_per_candidate), byref(a), ms, self.stream))
+        return a, np.array(ms[:], np.float64)
+
+    def time_phases(self, nsteps: int, flush_mb: int = 0) -> np.ndarray:
+        out = (c_float * 4)()
+        check(self._lib.arbo_batch_time_phases(self._h, int(nsteps), int(flush_mb), out, self.stream))
+        return np.array(out[:], np.float64)
+
+    def time_steps(self, nsteps: int, flush_mb: int = 0) -> np.ndarray:
+        out = np.zeros(int(nsteps), np.float32)
+        check(self._lib.arbo_batch_time_steps(self._h, int(nsteps), int(flush_mb), _f32p(out), self.stream))
+        return out.astype(np.float64)
+
+
 def simulation(parameter: Parameter, network: Network, max_time: int, n_sizes=None, m_sizes=None, seed: int = 0,
                sim_run: int = 0, mcmc_run: int = 0, write_output: bool = False, expected_mosquitoes=None
                ) -> Dict[str, np.ndarray]:

@@ -360,6 +360,42 @@ int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, voi
  */
 int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream);
 
+/* ------------------------------------------------------------------ batches */
+
+/* Many simulation handles stepped together: one persistent kernel per phase (demographic, force
+ * of infection, infection) walks the blocks of every instance, with the step loop captured in a
+ * CUDA graph. Replaces the reference's serial loop over replicates and MCMC proposals
+ * (cpp/main.cpp:262-280, one simulation() call each). Instances may differ in every size and
+ * parameter; each keeps its own buffers, key and counters, and its results are bit-identical to
+ * stepping it alone, so arbo_sim_get_* read them as usual. Instances are stepped only through the
+ * batch once it exists (they must stay at one step count) and outlive it. */
+typedef struct arbo_batch arbo_batch;
+
+/* Builds a batch of n handles (one device; each handle at most once). arch: launch shapes of the
+ * batched kernels (NULL: those of sims[0]); the grids are one wave of resident CTAs. */
+int arbo_batch_create(arbo_sim* const* sims, uint32_t n, const arbo_arch_param* arch, arbo_batch** out);
+int arbo_batch_destroy(arbo_batch* b);
+/* Number of instances and their total agents (humans + mosquito slots). */
+int arbo_batch_size(const arbo_batch* b, uint32_t* n, uint64_t* agents);
+/* arbo_sim_init of every instance. */
+int arbo_batch_init(arbo_batch* b, void* stream);
+/* Advances every instance by nsteps (clamped to the shortest remaining run). */
+int arbo_batch_step(arbo_batch* b, uint32_t nsteps, void* stream);
+int arbo_batch_run(arbo_batch* b, void* stream);
+/* Launch shapes: set (re-plans the block tables) and read back (grids[3] optional: CTAs of the
+ * three persistent kernels). */
+int arbo_batch_set_arch(arbo_batch* b, const arbo_arch_param* arch);
+int arbo_batch_get_arch(const arbo_batch* b, arbo_arch_param* arch, uint32_t grids[3]);
+/* Autotuner: tries demographic (block, unroll), force-of-infection block and infection block
+ * shapes in turn, each for steps_per_candidate real steps of the batch (the results do not depend
+ * on the shape), keeps the fastest per phase and applies it. Consumes 13*steps_per_candidate
+ * steps. best / best_ms (3 phase times of the choice, ms) are optional. */
+int arbo_batch_autotune(arbo_batch* b, uint32_t steps_per_candidate, arbo_arch_param* best, float* best_ms,
+                        void* stream);
+/* Measurement, as arbo_sim_time_phases / arbo_sim_time_steps for the whole batch. */
+int arbo_batch_time_phases(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* ms_out, void* stream);
+int arbo_batch_time_steps(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* step_ms, void* stream);
+
 /* ------------------------------------------------------------------ self-tests */
 
 /* Evaluate the device Philox4x32-10 on n (counter[4], key[2]) records packed as 6 uint32 each
