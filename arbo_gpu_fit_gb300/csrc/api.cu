@@ -1129,8 +1129,8 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     const uint32_t K = a.infectBlock >= 64 ? a.infectBlock / 64 : 1u;
     for (uint32_t i = 0; i < n; ++i) {
         const Dev& d = b->sims[i]->d;
-        const uint64_t hb = cdiv(d.nvec, (uint64_t)a.demogBlock * a.demogUnroll);
-        const uint64_t mb = cdiv(cdiv(d.tiles, kQuad), a.demogBlock / 32);
+        const uint64_t hb = cdiv(d.nvec, (uint64_t)32 * a.demogUnroll);  // warp items
+        const uint64_t mb = cdiv(d.tiles, kQuad);
         const uint64_t fb = cdiv((uint64_t)d.S * d.P, a.foiBlock / 4);
         const uint64_t ib = cdiv(d.P, K);
         if (demog_off[i] + hb + mb >= (1ull << 31) || foi_off[i] + fb >= (1ull << 31) ||
@@ -1144,7 +1144,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     uint32_t occ[3] = {1, 1, 1};
     const int oe = batch_blocks_per_sm(l, occ);
     if (oe) return fail(ARBO_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString((cudaError_t)oe));
-    const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3) * 4;
+    const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3 + 1) * 4;
     if (!b->mem) CUDA_TRY(cudaMalloc(&b->mem, devb + tab));
     std::vector<Dev> devs(n);
     for (uint32_t i = 0; i < n; ++i) devs[i] = b->sims[i]->d;
@@ -1154,6 +1154,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     t.insert(t.end(), demog_h.begin(), demog_h.end());
     t.insert(t.end(), foi_off.begin(), foi_off.end());
     t.insert(t.end(), infect_off.begin(), infect_off.end());
+    t.push_back(0u);  // demographic work counter
     CUDA_TRY(cudaMemcpy(b->mem, devs.data(), sizeof(Dev) * n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy((char*)b->mem + devb, t.data(), tab, cudaMemcpyHostToDevice));
     uint32_t* tp = (uint32_t*)((char*)b->mem + devb);
@@ -1163,6 +1164,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     bd.demog_h = tp + (n + 1);
     bd.foi_off = tp + (2 * n + 1);
     bd.infect_off = tp + (3 * n + 2);
+    bd.work = tp + (4 * n + 3);
     bd.n = n;
     b->blocks[0] = demog_off[n];
     b->blocks[1] = foi_off[n];

@@ -1104,19 +1104,55 @@ __device__ __forceinline__ void batch_loop(const BatchDev& bd, const uint32_t* _
     }
 }
 
+// Demographic pass of a batch. Work items are per warp: 32*U-lane groups of humans or one
+// mosquito quad, instance by instance (bd.demog_off counts warp items, bd.demog_h the human items
+// of each instance). Warps take pairs of consecutive items from a device counter (reset by the
+// force-of-infection kernel once this kernel has finished), so uneven instances balance across
+// the GPU, and each warp keeps a private copy of its current instance's descriptor in shared
+// memory: no block-wide barrier anywhere.
 template <int U>
 __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t koff)
 {
     __shared__ QuadSmem wsm[8];
-    batch_loop(bd, bd.demog_off, [&](const Dev& d, uint32_t inst, uint32_t b) {
-        demog_block<U>(d, b, __ldg(&bd.demog_h[inst]), koff, wsm);
-    });
+    __shared__ __align__(16) unsigned long long wdev[8][sizeof(Dev) / 8];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const Dev& d = *reinterpret_cast<const Dev*>(wdev[warp]);
+    const uint32_t total = __ldg(&bd.demog_off[bd.n]);
+    uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its item range
+    for (;;) {
+        uint32_t it0 = 0;
+        if (lane == 0) it0 = atomicAdd(bd.work, 2u);
+        it0 = __shfl_sync(kFull, it0, 0);
+        if (it0 >= total) break;
+        for (uint32_t it = it0; it < it0 + 2 && it < total; ++it) {
+            if (inst == UINT_MAX || it >= hi) {
+                // Items arrive in increasing order: usually the next instance, else search.
+                const bool next = inst != UINT_MAX && inst + 2 <= bd.n && it < __ldg(&bd.demog_off[inst + 2]);
+                inst = next ? inst + 1 : batch_instance(bd.demog_off, bd.n, it);
+                lo = __ldg(&bd.demog_off[inst]);
+                hi = __ldg(&bd.demog_off[inst + 1]);
+                __syncwarp();
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
+                for (uint32_t i = lane; i < sizeof(Dev) / 8; i += 32) wdev[warp][i] = src[i];
+                __syncwarp();
+            }
+            const uint32_t local = it - lo, hw = __ldg(&bd.demog_h[inst]);
+            const uint32_t t = d.ctrl->t + koff;
+            const Key key = load_key(d.ctrl);
+            if (local < hw) demog_humans<U>(d, key, local * 32 * U + lane, 32, t);
+            else demog_mosquito_quad(d, key, local - hw, lane, t, wsm[warp]);
+        }
+    }
     griddep_launch_dependents();
 }
 
 __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
 {
     __shared__ FoiSmem fs;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        griddep_wait();  // the demographic kernel has finished taking items
+        *bd.work = 0u;
+    }
     batch_loop(bd, bd.foi_off, [&](const Dev& d, uint32_t, uint32_t b) { foi_block(d, b, 0, koff, fs); });
 }
 

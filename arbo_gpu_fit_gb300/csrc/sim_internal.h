@@ -110,8 +110,9 @@ static_assert(sizeof(Dev) % 16 == 0 || sizeof(Dev) % 8 == 0, "Dev is staged into
 // the concatenation of the instances' blocks; off arrays hold each instance's first block.
 struct BatchDev {
     const Dev* devs;             // [n] descriptors in device memory
-    const uint32_t* demog_off;   // [n+1] demographic blocks
-    const uint32_t* demog_h;     // [n] human blocks of each instance (the rest are mosquito blocks)
+    const uint32_t* demog_off;   // [n+1] demographic warp items (32*U-lane human groups, mosquito quads)
+    const uint32_t* demog_h;     // [n] human warp items of each instance (the rest are quads)
+    uint32_t* work;              // demographic item counter (zero between steps)
     const uint32_t* foi_off;     // [n+1] force-of-infection blocks
     const uint32_t* infect_off;  // [n+1] infection blocks (K communities each)
     uint32_t n;

@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--e2e-runs", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="profile-sized workload (1/8 of the large one)")
+    ap.add_argument("--batched-instances", type=int, default=256,
+                    help="instances of the batched configuration measured beside the headline (0: skip)")
+    ap.add_argument("--batched-steps", type=int, default=40)
     ap.add_argument("--ref-gpu-steps", type=int, default=-1,
                     help="steps of the reference's own CUDA kernels timed in the reference arm "
                          "(-1: the same as --steps after --warmup untimed steps; 0: skip)")
@@ -323,12 +326,59 @@ def ours_arm(args, world, rank, local):
         "gpu_launches": 4 * K + -(-K // 64),
         "gpu_launches_detail": {"step_kernels": 3 * K, "l2_flush_kernels": K, "step_counter_kernels": -(-K // 64)},
     }
+    if args.batched_instances > 0:
+        line["batched"] = batched_measure(args, seed)
     if world == 1 and not args.no_cpu_baseline:
         rate, per_step_ms, _ = cpu_baseline(args, 1)
         line["cpu_baseline"] = {"value": rate, "unit": "agent-steps/s", "cores": 1, "kind": "port",
                                 "sample": f"init (untimed) + {args.cpu_steps} serial steps of the same workload, "
                                           f"oracle/ restatement on 1 host core ({per_step_ms:.0f} ms/step)"}
     print(json.dumps(line), flush=True)
+
+
+def batched_measure(args, seed):
+    """The batched configuration: independent instances of uneven sizes and parameters advanced by
+    one persistent kernel per phase (arbo_batch_*), launch shapes picked by the autotuner, against
+    the same instances stepped one at a time (one graph-launched handle after another). The working
+    set is far larger than L2, so no flush is needed."""
+    from arbo_gpu_fit_gb300 import configs
+    from arbo_gpu_fit_gb300.simulation import Batch, Simulation
+
+    ws = configs.batched(args.batched_instances, seed=seed)
+    t0 = time.perf_counter()
+    sims = [Simulation(w.parameter, w.network, w.n_sizes, w.m_sizes, max_time=w.max_time, seed=w.seed) for w in ws]
+    create_s = time.perf_counter() - t0
+    K = args.batched_steps
+    with Batch(sims) as b:
+        agents = b.agents
+        b.init()
+        arch, tuned_ms = b.autotune(2)
+        b.step(3)
+        step_ms = b.time_steps(K)
+        phases = b.time_phases(5)
+        grids = b.arch()[1]
+    batched_s = float(step_ms.sum()) / 1e3
+    # The same instances, one after another, each graph-launched (same step range: the batch left
+    # every instance at the same step).
+    seq_ms = 0.0
+    for s in sims:
+        seq_ms += float(s.time_steps(K).sum())
+    for s in sims:
+        s.close()
+    return {
+        "workload": (f"{len(ws)} instances: humans log-uniform [2e4, 2e6], 6 mosquito slots per human, communities "
+                     "log-uniform [100, 4000] on near-square rook lattices, 4 serotypes, 1,825 steps/run, "
+                     "parameters uniform in the MCMC prior box"),
+        "instances": len(ws), "agents": agents, "steps": K,
+        "value": agents * K / batched_s, "unit": "agent-steps/s", "ms_per_step": batched_s * 1e3 / K,
+        "sequential_value": agents * K / (seq_ms / 1e3), "speedup_vs_sequential": (seq_ms / 1e3) / batched_s,
+        "roofline_frac_step": BYTES_PER_AGENT_STEP * agents * K / batched_s / 1e9 / hbm_peak()[0],
+        "phase_ms": {"demographic": phases[0], "foi_series": phases[1], "infection": phases[2], "step": phases[3]},
+        "autotuned": {"demogBlock": arch.demogBlock, "demogUnroll": arch.demogUnroll, "foiBlock": arch.foiBlock,
+                      "infectBlock": arch.infectBlock, "grids": grids, "phase_ms": tuned_ms.tolist()},
+        "create_s": create_s,
+        "timing": "CUDA events around each graph-launched batch step; no L2 flush (working set >> L2)",
+    }
 
 
 def main():
