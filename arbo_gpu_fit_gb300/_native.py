@@ -43,6 +43,14 @@ class IOParamStruct(ctypes.Structure):
     _fields_ = [("idir", c_char_p), ("iClimateFile", c_char_p), ("iDengueFile", c_char_p), ("odir", c_char_p)]
 
 
+class McmcConfigStruct(ctypes.Structure):
+    _fields_ = [("chains", c_uint32), ("params", c_uint32), ("replicates", c_uint32), ("months", c_uint32),
+                ("serotypes", c_uint32), ("max_iters", c_uint32), ("report_param", c_uint32), ("reserved", c_uint32),
+                ("lo", POINTER(ctypes.c_double)), ("hi", POINTER(ctypes.c_double)), ("step", POINTER(ctypes.c_double)),
+                ("observed", POINTER(c_uint32)), ("month_start", POINTER(c_uint32)), ("nb_size", ctypes.c_double),
+                ("seed", c_uint64)]
+
+
 class CSRStruct(ctypes.Structure):
     _fields_ = [("subPopTotal", c_uint32), ("nnz", c_uint32), ("loc", POINTER(c_uint32)), ("to", POINTER(c_uint32)),
                 ("weight", POINTER(c_float))]
@@ -100,6 +108,17 @@ SIGNATURES = {
     "arbo_sim_write_incidence": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
     "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
+    "arbo_sim_set_param": (c_int, [c_void_p, POINTER(SimParamStruct)]),
+    "arbo_mcmc_create": (c_int, [POINTER(McmcConfigStruct), POINTER(c_void_p)]),
+    "arbo_mcmc_destroy": (c_int, [c_void_p]),
+    "arbo_mcmc_set_state": (c_int, [c_void_p, POINTER(ctypes.c_double), c_void_p]),
+    "arbo_mcmc_propose": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_double), c_void_p]),
+    "arbo_mcmc_loglik": (c_int, [c_void_p, POINTER(c_void_p), c_uint32, c_uint32, c_int, c_void_p]),
+    "arbo_mcmc_accept": (c_int, [c_void_p, c_uint32, c_uint32, c_uint32, c_int, c_void_p]),
+    "arbo_mcmc_set_screen": (c_int, [c_void_p, POINTER(ctypes.c_double), POINTER(ctypes.c_double), c_void_p]),
+    "arbo_mcmc_screen": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_uint8), c_void_p]),
+    "arbo_mcmc_state": (c_int, [c_void_p, POINTER(ctypes.c_double), POINTER(ctypes.c_double), POINTER(ctypes.c_double), POINTER(c_uint32), POINTER(c_uint32)]),
+    "arbo_mcmc_chain": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_double), POINTER(ctypes.c_uint8)]),
     "arbo_batch_create": (c_int, [POINTER(c_void_p), c_uint32, POINTER(ArchParamStruct), POINTER(c_void_p)]),
     "arbo_batch_destroy": (c_int, [c_void_p]),
     "arbo_batch_size": (c_int, [c_void_p, POINTER(c_uint32), POINTER(c_uint64)]),

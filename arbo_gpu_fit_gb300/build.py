@@ -19,7 +19,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "libarbo_gb300.so"
-SOURCES = ["kernels.cu", "api.cu", "selftest.cu"]
+SOURCES = ["kernels.cu", "api.cu", "mcmc.cu", "selftest.cu"]
 HEADERS = ["philox.cuh", "sim_internal.h"]
 INCLUDE = PKG.parent / "include"
 

@@ -66,6 +66,40 @@ std::vector<float> cdf_table(const arbo_sim_param& p, bool human, uint32_t max_a
 
 float table_at(const std::vector<float>& t, uint32_t a) { return t[std::min<size_t>(a, t.size() - 1)]; }
 
+// Expected live mosquitoes E[t], t = 0..T: mosBaseRatio * N * (1 + seasonAmp * sin(2 pi (t - phase) / 365)),
+// in double, capped at the slot count, rounded once.
+void fill_expected(const arbo_sim_param& p, uint32_t M, uint32_t T, std::vector<float>& etab)
+{
+    etab.resize(T + 1);
+    for (uint32_t t = 0; t <= T; ++t) {
+        double e = (double)p.mosBaseRatio * (double)p.nSize *
+                   (1.0 + (double)p.seasonAmp * std::sin(2.0 * 3.14159265358979323846 * ((double)t - (double)p.seasonPhase) / 365.0));
+        e = std::min(e, (double)M);
+        e = std::max(e, 0.0);
+        etab[t] = (float)e;
+    }
+}
+
+// The parameters the kernels read from the descriptor.
+void apply_rates(const arbo_sim_param& p, Dev& d)
+{
+    d.biting = p.bitingRate;
+    d.mnSuccess = p.mnBitingSuccess;
+    d.nmSuccess = p.nmBitingSuccess;
+    d.recovery = p.recovery;
+    d.mExposed = p.mExposed;
+    d.nExposed = p.nExposed;
+    d.extInf = p.externalInfection;
+    d.longDist = p.longDistance;
+    d.noDist = p.noDistance;
+    d.seroPrev = p.initialSeroPrev;
+    d.maxIntro = p.maxIntroAttempt;
+    d.maxTarget = p.maxTargetAttempt;
+    d.quirks = p.quirks;
+    d.nInit = std::min<uint32_t>((uint32_t)p.nInitialInf, d.N);
+    d.mInit = std::min<uint32_t>((uint32_t)p.mInitialInf, d.M);
+}
+
 uint32_t comm_of_host(const std::vector<uint32_t>& loc, uint32_t P, uint32_t i)
 {
     uint32_t lo = 0, hi = P;
@@ -101,6 +135,7 @@ struct arbo_sim {
     void* flush = nullptr;           // L2 flush buffer (measurement only)
     size_t flush_bytes = 0;
     std::vector<cudaEvent_t> step_ev;  // per-step event pairs of arbo_sim_time_steps
+    uint64_t version = 0;              // bumped when the parameters in d change
 };
 
 extern "C" {
@@ -351,14 +386,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     for (uint32_t y = 1; y <= p.nMaxInitialAgeYears; ++y) survh[y] = survh[y - 1] + (1.0f - table_at(cdfh, 365u * y));
     survm[0] = 1.0f - table_at(cdfm, 0);
     for (uint32_t a = 1; a <= p.mMaxInitialAge; ++a) survm[a] = survm[a - 1] + (1.0f - table_at(cdfm, a));
-    s->etab.resize(T + 1);
-    for (uint32_t t = 0; t <= T; ++t) {
-        double e = (double)p.mosBaseRatio * (double)p.nSize *
-                   (1.0 + (double)p.seasonAmp * std::sin(2.0 * 3.14159265358979323846 * ((double)t - (double)p.seasonPhase) / 365.0));
-        e = std::min(e, (double)M);
-        e = std::max(e, 0.0);
-        s->etab[t] = (float)e;
-    }
+    fill_expected(p, M, T, s->etab);
 
     Dev& d = s->d;
     d.N = N;
@@ -373,22 +401,8 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     d.am = (uint32_t)cdfm.size();
     d.yh = p.nMaxInitialAgeYears;
     d.dm = p.mMaxInitialAge;
-    d.biting = p.bitingRate;
-    d.mnSuccess = p.mnBitingSuccess;
-    d.nmSuccess = p.nmBitingSuccess;
-    d.recovery = p.recovery;
-    d.mExposed = p.mExposed;
-    d.nExposed = p.nExposed;
-    d.extInf = p.externalInfection;
-    d.longDist = p.longDistance;
-    d.noDist = p.noDistance;
-    d.seroPrev = p.initialSeroPrev;
-    d.maxIntro = p.maxIntroAttempt;
-    d.maxTarget = p.maxTargetAttempt;
-    d.quirks = p.quirks;
+    apply_rates(p, d);
     d.recordSpatial = p.recordSpatial ? 1u : 0u;
-    d.nInit = std::min<uint32_t>((uint32_t)p.nInitialInf, N);
-    d.mInit = std::min<uint32_t>((uint32_t)p.mInitialInf, M);
 
     // One allocation, every array 256-byte aligned.
     const size_t Np = (size_t)d.nvec * 4, Mp = (size_t)d.tiles * kTile, SP = (size_t)S * P, R = (size_t)T + 1;
@@ -515,6 +529,41 @@ int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* e, size_t n)
     }
     CUDA_TRY(cudaMemcpy(s->d.etab, s->etab.data(), n * 4, cudaMemcpyHostToDevice));
     s->h2d += n * 4;
+    return ARBO_OK;
+}
+
+int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p)
+{
+    if (!s || !p) return fail(ARBO_ERR_INVALID, "null argument");
+    const arbo_sim_param& o = s->p;
+    // Sizes, life expectancies and table ranges fix the allocation and the tables.
+    const bool same_shape = p->nSize == o.nSize && p->metaPop == o.metaPop && p->mSize == o.mSize &&
+                            p->nStrains == o.nStrains && p->nShapeInfantMortality == o.nShapeInfantMortality &&
+                            p->nScaleInfantMortality == o.nScaleInfantMortality &&
+                            p->nScaleLifeExpectancy == o.nScaleLifeExpectancy &&
+                            p->nShapeLifeExpectancy == o.nShapeLifeExpectancy && p->nLocWeibull == o.nLocWeibull &&
+                            p->mScaleLifeExpectancy == o.mScaleLifeExpectancy &&
+                            p->mShapeLifeExpectancy == o.mShapeLifeExpectancy &&
+                            p->nMaxInitialAgeYears == o.nMaxInitialAgeYears && p->mMaxInitialAge == o.mMaxInitialAge &&
+                            p->recordSpatial == o.recordSpatial && p->nHeteroPopSize == o.nHeteroPopSize &&
+                            p->mHeteroPopSize == o.mHeteroPopSize;
+    if (!same_shape)
+        return fail(ARBO_ERR_INVALID, "arbo_sim_set_param changes only transmission, dispersal, seeding, seasonal "
+                                      "and attempt parameters; sizes and life expectancies need a new handle");
+    if (p->maxTargetAttempt < 1 || p->maxTargetAttempt > (1u << 18) || p->maxIntroAttempt > (1u << 26))
+        return fail(ARBO_ERR_INVALID, "attempt limits out of range");
+    CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // no step of this handle may be reading the old series
+    s->p = *p;
+    apply_rates(*p, s->d);
+    fill_expected(*p, s->d.M, s->d.T, s->etab);
+    CUDA_TRY(cudaMemcpy(s->d.etab, s->etab.data(), s->etab.size() * 4, cudaMemcpyHostToDevice));
+    s->h2d += s->etab.size() * 4;
+    // Captured graphs hold the old descriptor.
+    if (s->gmulti) cudaGraphExecDestroy(s->gmulti);
+    if (s->gone) cudaGraphExecDestroy(s->gone);
+    s->gmulti = s->gone = nullptr;
+    s->version += 1;
     return ARBO_OK;
 }
 
@@ -1092,6 +1141,7 @@ struct arbo_batch {
     std::vector<cudaEvent_t> step_ev;
     void* flush = nullptr;
     size_t flush_bytes = 0;
+    std::vector<uint64_t> versions;  // instance versions the uploaded descriptors reflect
 };
 
 namespace {
@@ -1147,7 +1197,11 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3 + 1) * 4;
     if (!b->mem) CUDA_TRY(cudaMalloc(&b->mem, devb + tab));
     std::vector<Dev> devs(n);
-    for (uint32_t i = 0; i < n; ++i) devs[i] = b->sims[i]->d;
+    b->versions.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        devs[i] = b->sims[i]->d;
+        b->versions[i] = b->sims[i]->version;
+    }
     std::vector<uint32_t> t;
     t.reserve(4 * n + 3);
     t.insert(t.end(), demog_off.begin(), demog_off.end());
@@ -1179,8 +1233,21 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     return ARBO_OK;
 }
 
+// Re-uploads the descriptors of instances whose parameters changed (arbo_sim_set_param).
+int batch_refresh(arbo_batch* b)
+{
+    for (size_t i = 0; i < b->sims.size(); ++i) {
+        if (b->versions[i] == b->sims[i]->version) continue;
+        CUDA_TRY(cudaMemcpy((Dev*)b->mem + i, &b->sims[i]->d, sizeof(Dev), cudaMemcpyHostToDevice));
+        b->versions[i] = b->sims[i]->version;
+    }
+    return ARBO_OK;
+}
+
 int batch_ready(arbo_batch* b, uint32_t* t_out)
 {
+    const int re = batch_refresh(b);
+    if (re) return re;
     uint32_t t = 0;
     for (size_t i = 0; i < b->sims.size(); ++i) {
         const arbo_sim* s = b->sims[i];
@@ -1502,3 +1569,18 @@ int arbo_batch_autotune(arbo_batch* b, uint32_t steps_per_candidate, arbo_arch_p
 }
 
 }  // extern "C"
+
+namespace arbo {
+
+const uint32_t* sim_incidence_series(const arbo_sim* s, uint32_t* T, uint32_t* S)
+{
+    *T = s->d.T;
+    *S = s->d.S;
+    return s->d.s_ninc;
+}
+
+int sim_device(const arbo_sim* s) { return s->device; }
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+}  // namespace arbo

@@ -42,7 +42,10 @@ enum Stream : uint32_t {
     kInfHExposed = 19,   // per human event: rounding of exposed and recovery ages
     kIntroCount = 20,    // per (serotype, community): number of external introductions
     kIntroTarget = 21,   // per introduction attempt: target
-    kIntroExposed = 22   // per introduction attempt: rounding of exposed and recovery ages
+    kIntroExposed = 22,  // per introduction attempt: rounding of exposed and recovery ages
+    kMcmcPropose = 23,   // per (chain, iteration), sub = parameter: Gaussian random-walk step
+    kMcmcAccept = 24,    // per (chain, iteration): Metropolis-Hastings uniform
+    kMcmcScreen = 25     // per (chain, iteration): first-stage uniform of delayed acceptance
 };
 
 struct U4 {
@@ -98,6 +101,12 @@ ARBO_HD U4 draw4(const Key& key, uint32_t stream, uint32_t entity, uint32_t step
 
 // Uniform in (0, 1], the range of curand_uniform; exact in single precision.
 ARBO_HD float u01(uint32_t x) { return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f); }
+
+// Uniform in (0, 1] with 53 random bits from two words; exact in double precision.
+ARBO_HD double u01d(uint32_t hi, uint32_t lo)
+{
+    return ((double)(hi >> 5) * 67108864.0 + (double)(lo >> 6) + 1.0) * (1.0 / 9007199254740992.0);
+}
 
 // Integer in [0, n): the high word of x * n (stands in for curand() % n).
 ARBO_HD uint32_t bounded(uint32_t x, uint32_t n) { return mulhi32(x, n); }

@@ -18,7 +18,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "philox.cuh"
+
+struct arbo_sim;  // include/arbo.h
 
 namespace arbo {
 
@@ -141,6 +145,13 @@ uint32_t launches_per_step();
 // Batched steps (see BatchDev); the block shapes come from l, the grids from bd.
 int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* events, uint32_t koff);
 int launch_advance_batch(const BatchDev& bd, uint32_t n, void* stream);
+// Records the message returned by arbo_last_error (api.cu) and returns code.
+int set_error(int code, const std::string& msg);
+
+// Daily incidence series of a handle ([T+1][S], device) and its device (api.cu).
+const uint32_t* sim_incidence_series(const arbo_sim* s, uint32_t* T, uint32_t* S);
+int sim_device(const arbo_sim* s);
+
 // Resident CTAs per SM of the three batched kernels for the block shapes of l.
 int batch_blocks_per_sm(const Launch& l, uint32_t out[3]);
 // Reads `bytes` of buf (a multiple of 16) to evict L2; `sink` is a device word never written in practice.

@@ -1,0 +1,336 @@
+"""MCMC over the simulator: the host driver of the reference's MCMC class (cpp/MCMC.h, cpp/MCMC.cpp,
+cpp/main.cpp:72-350) over the C-ABI.
+
+Each iteration: ``propose`` (GPU, keyed Philox), ``copy_params`` of every chain's proposal into its
+simulation handles (arbo_sim_set_param), the simulations, ``calc_log_likelihood`` (GPU, FP64
+negative-binomial over months and serotypes, log-mean-exp over replicates) and ``next_step``
+(GPU, FP64 Metropolis-Hastings). Three drivers share those calls:
+
+* ``run_plain``: one proposal at a time, one simulation handle reused chain after chain;
+* ``run_batched``: every chain's proposal simulated together by one batch (arbo_batch_*);
+* ``run_delayed``: delayed acceptance, a surrogate log-likelihood screens the proposals first
+  and only those that pass are simulated.
+
+The parameter vector is the prior box of the fit (configs.PRIOR_BOX): human-to-mosquito and
+mosquito-to-human transmission, local dispersal fraction, seasonal amplitude and phase (the
+simulation's), and the reporting rate (the observation model's).
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from ctypes import POINTER, byref, c_uint32, c_void_p
+from typing import Callable, List, Optional
+
+import numpy as np
+
+from . import configs
+from ._native import McmcConfigStruct, check, load
+from .simulation import Batch, Simulation
+
+_D = POINTER(ctypes.c_double)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def month_rows(max_time: int, months: int) -> np.ndarray:
+    """First row of each period in the daily incidence series (row t+1 = step t), plus the end:
+    period m covers steps floor(m*T/months) .. floor((m+1)*T/months) - 1."""
+    b = (np.arange(months + 1, dtype=np.int64) * max_time) // months
+    return (b + 1).astype(np.uint32)
+
+
+def monthly(daily: np.ndarray, rows: np.ndarray) -> np.ndarray:
+    """(T+1, S) daily series -> (months, S) sums over the rows of each period."""
+    c = np.concatenate([np.zeros((1, daily.shape[1]), np.int64), np.cumsum(daily.astype(np.int64), axis=0)])
+    return (c[rows[1:]] - c[rows[:-1]]).astype(np.int64)
+
+
+def synthetic_data(workload: configs.Workload, theta_true, months: int = 120, nb_size: float = 10.0,
+                   seed: int = 0, report_param: int = 5) -> np.ndarray:
+    """Observed monthly cases per serotype: the workload simulated at theta_true, times the
+    reporting rate, with negative-binomial noise of the given size (numpy, seeded)."""
+    sp = configs.apply_theta(workload.parameter.simulation, theta_true)
+    with Simulation(_with_sim(workload.parameter, sp), workload.network, workload.n_sizes, workload.m_sizes,
+                    max_time=workload.max_time, seed=workload.seed) as sim:
+        sim.init()
+        sim.run()
+        daily = sim.series("n_incidence")
+    mean = float(theta_true[report_param]) * monthly(daily, month_rows(workload.max_time, months))
+    rng = np.random.default_rng(seed)
+    p = nb_size / (nb_size + mean)
+    return rng.negative_binomial(nb_size, p).astype(np.uint32)
+
+
+def _with_sim(parameter, sp):
+    from .simulation import Parameter
+
+    return Parameter(sp, parameter.arch, parameter.io)
+
+
+class MCMC:
+    """Chains of the fit (the reference's MCMC class) with their state on the GPU."""
+
+    def __init__(self, workload: configs.Workload, observed: np.ndarray, chains: int, step, seed: int = 1,
+                 replicates: int = 1, max_iters: int = 1000, nb_size: float = 10.0, box=None, report_param: int = 5):
+        self._lib = load()
+        self.workload = workload
+        box = box if box is not None else configs.PRIOR_BOX
+        self.lo = np.array([b[1] for b in box], np.float64)
+        self.hi = np.array([b[2] for b in box], np.float64)
+        self.step_sd = np.ascontiguousarray(step, np.float64)
+        self.C, self.D, self.R = int(chains), len(box), int(replicates)
+        self.observed = np.ascontiguousarray(observed, np.uint32)
+        self.months = int(self.observed.shape[0])
+        self.S = int(self.observed.shape[1])
+        self.rows = month_rows(workload.max_time, self.months)
+        self.max_iters = int(max_iters)
+        cfg = McmcConfigStruct(self.C, self.D, self.R, self.months, self.S, self.max_iters, int(report_param), 0,
+                               _dp(self.lo), _dp(self.hi), _dp(self.step_sd),
+                               self.observed.ctypes.data_as(POINTER(c_uint32)),
+                               self.rows.ctypes.data_as(POINTER(c_uint32)), float(nb_size), int(seed))
+        h = c_void_p()
+        check(self._lib.arbo_mcmc_create(byref(cfg), byref(h)))
+        self._h = h
+        self.base = workload.parameter.simulation
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.arbo_mcmc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the reference's MCMC member functions ------------------------------------------
+    def set_state(self, theta: np.ndarray) -> None:
+        t = np.ascontiguousarray(theta, np.float64).reshape(self.C, self.D)
+        check(self._lib.arbo_mcmc_set_state(self._h, _dp(t), None))
+
+    def propose(self, it: int) -> np.ndarray:
+        out = np.zeros((self.C, self.D), np.float64)
+        check(self._lib.arbo_mcmc_propose(self._h, int(it), _dp(out), None))
+        return out
+
+    def check_params(self, theta: np.ndarray) -> np.ndarray:
+        """True where a proposal lies inside the prior box (MCMC::checkParams, cpp/MCMC.cpp:139-159)."""
+        return np.all((theta >= self.lo) & (theta <= self.hi), axis=-1)
+
+    def copy_params(self, sim: Simulation, theta, chain: int, replicate: int, it: int) -> None:
+        """MCMC::copyParams (cpp/MCMC.cpp:75-82): the proposal's simulation parameters into a handle,
+        and the simulation seed of (chain, replicate, iteration) — fresh randomness for every
+        proposal, as the reference reseeds every run. Out-of-box values are clamped for the
+        simulation; such proposals are rejected anyway."""
+        th = np.clip(np.asarray(theta, np.float64), self.lo, self.hi)
+        sp = configs.apply_theta(self.base, th)
+        check(self._lib.arbo_sim_set_param(sim._h, byref(sp)))
+        sim.set_seed(sim_seed(self.workload.seed, chain, replicate, it))
+
+    def calc_log_likelihood(self, sims: List[Simulation], c0: int, c1: int, current: bool = False) -> None:
+        hs = (c_void_p * len(sims))(*[s._h.value for s in sims])
+        check(self._lib.arbo_mcmc_loglik(self._h, hs, int(c0), int(c1), int(current), None))
+
+    def next_step(self, it: int, c0: int = 0, c1: Optional[int] = None, screened: bool = False) -> None:
+        check(self._lib.arbo_mcmc_accept(self._h, int(it), int(c0), int(self.C if c1 is None else c1), int(screened),
+                                         None))
+
+    def set_screen(self, screen_prop: np.ndarray, screen_cur: Optional[np.ndarray] = None) -> None:
+        a = np.ascontiguousarray(screen_prop, np.float64)
+        b = np.ascontiguousarray(screen_cur, np.float64) if screen_cur is not None else None
+        check(self._lib.arbo_mcmc_set_screen(self._h, _dp(a), _dp(b) if b is not None else None, None))
+
+    def screen(self, it: int) -> np.ndarray:
+        out = np.zeros(self.C, np.uint8)
+        check(self._lib.arbo_mcmc_screen(self._h, int(it), out.ctypes.data_as(POINTER(ctypes.c_uint8)), None))
+        return out.astype(bool)
+
+    def state(self):
+        th = np.zeros((self.C, self.D), np.float64)
+        lp, ll = np.zeros(self.C), np.zeros(self.C)
+        acc, pas = np.zeros(self.C, np.uint32), np.zeros(self.C, np.uint32)
+        check(self._lib.arbo_mcmc_state(self._h, _dp(th), _dp(lp), _dp(ll), acc.ctypes.data_as(POINTER(c_uint32)),
+                                        pas.ctypes.data_as(POINTER(c_uint32))))
+        return {"theta": th, "logpost": lp, "loglik": ll, "accepted": acc, "passed": pas}
+
+    def chain(self, iters: int):
+        out = np.zeros((iters, self.C, self.D), np.float64)
+        fl = np.zeros((iters, self.C), np.uint8)
+        check(self._lib.arbo_mcmc_chain(self._h, int(iters), _dp(out), fl.ctypes.data_as(POINTER(ctypes.c_uint8))))
+        return out, fl.astype(bool)
+
+    # -- helpers shared by the drivers ----------------------------------------------------
+    def make_sims(self, n: int) -> List[Simulation]:
+        w = self.workload
+        return [Simulation(w.parameter, w.network, w.n_sizes, w.m_sizes, max_time=w.max_time, seed=w.seed + k)
+                for k in range(n)]
+
+
+def sim_seed(base: int, chain: int, replicate: int, it: int) -> int:
+    """Simulation seed of (chain, replicate, iteration)."""
+    x = (int(base) * 0x9E3779B97F4A7C15 + (it << 40) + (chain << 16) + replicate) & (2**64 - 1)
+    x ^= x >> 31
+    return (x * 0xBF58476D1CE4E5B9) & (2**64 - 1)
+
+
+def _simulate_alone(sim: Simulation):
+    sim.init()
+    sim.run()
+
+
+def start(m: MCMC, theta0: np.ndarray, sims: List[Simulation], batch: Optional[Batch] = None) -> None:
+    """Iteration 0: evaluates the initial states (current = 1) and records them."""
+    m.set_state(theta0)
+    theta0 = np.asarray(theta0).reshape(m.C, m.D)
+    if batch is None:
+        for c in range(m.C):
+            for r in range(m.R):
+                m.copy_params(sims[r], theta0[c], c, r, 0)
+                _simulate_alone(sims[r])
+            m.calc_log_likelihood(sims[:m.R], c, c + 1, current=True)
+    else:
+        for c in range(m.C):
+            for r in range(m.R):
+                m.copy_params(sims[c * m.R + r], theta0[c], c, r, 0)
+        batch.init()
+        batch.run()
+        m.calc_log_likelihood(sims, 0, m.C, current=True)
+
+
+def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
+              on_iter: Optional[Callable] = None) -> dict:
+    """One proposal at a time: for every chain in turn, its proposal is simulated by the same
+    handle(s) (replicates of one handle each) and accepted or rejected."""
+    sims = sims if sims is not None else m.make_sims(m.R)
+    t0 = time.perf_counter()
+    start(m, theta0, sims)
+    sim_s = 0.0
+    for it in range(1, iters):
+        prop = m.propose(it)
+        for c in range(m.C):
+            t1 = time.perf_counter()
+            for r in range(m.R):
+                m.copy_params(sims[r], prop[c], c, r, it)
+                _simulate_alone(sims[r])
+            sim_s += time.perf_counter() - t1
+            m.calc_log_likelihood(sims[:m.R], c, c + 1)
+            m.next_step(it, c, c + 1)
+        if on_iter:
+            on_iter(it)
+    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * iters}
+
+
+def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
+                batch: Optional[Batch] = None, on_iter: Optional[Callable] = None) -> dict:
+    """All chains together: the proposals of the C chains (times replicates) are simulated by one
+    batch, then the likelihoods and the acceptance steps of all chains run as one kernel each."""
+    sims = sims if sims is not None else m.make_sims(m.C * m.R)
+    own = batch is None
+    batch = batch if batch is not None else Batch(sims)
+    t0 = time.perf_counter()
+    start(m, theta0, sims, batch)
+    sim_s = 0.0
+    for it in range(1, iters):
+        prop = m.propose(it)
+        for c in range(m.C):
+            for r in range(m.R):
+                m.copy_params(sims[c * m.R + r], prop[c], c, r, it)
+        t1 = time.perf_counter()
+        batch.init()
+        batch.run()
+        sim_s += time.perf_counter() - t1
+        m.calc_log_likelihood(sims, 0, m.C)
+        m.next_step(it)
+        if on_iter:
+            on_iter(it)
+    if own:
+        batch.close()
+    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * iters}
+
+
+def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np.ndarray], np.ndarray],
+                sims: Optional[List[Simulation]] = None, on_iter: Optional[Callable] = None) -> dict:
+    """Delayed-acceptance Metropolis-Hastings (Christen & Fox 2005). ``surrogate(theta[C, D])``
+    returns an approximate log-likelihood per chain. Stage 1 screens every proposal with it (GPU,
+    FP64); only the proposals that pass are simulated, together in one batch of as many handles as
+    there are passing chains (replicates each), and stage 2 accepts them with the simulator's
+    likelihood divided by the surrogate's. The simulator stays the judge: a proposal is accepted
+    only on its simulated likelihood."""
+    sims = sims if sims is not None else m.make_sims(m.C * m.R)
+    t0 = time.perf_counter()
+    theta0 = np.asarray(theta0, np.float64).reshape(m.C, m.D)
+    with Batch(sims) as b0:
+        start(m, theta0, sims, b0)
+    m.set_screen(surrogate(theta0), surrogate(theta0))
+    sim_s, simulated = 0.0, m.C * m.R
+    batches = {}
+    try:
+        for it in range(1, iters):
+            prop = m.propose(it)
+            m.set_screen(surrogate(prop))
+            passed = np.flatnonzero(m.screen(it))
+            if passed.size:
+                n = passed.size
+                if n not in batches:
+                    batches[n] = Batch(sims[: n * m.R])
+                # Handle rows of the passing chains: the first n*R handles, in chain order.
+                for j, c in enumerate(passed):
+                    for r in range(m.R):
+                        m.copy_params(sims[j * m.R + r], prop[c], int(c), r, it)
+                t1 = time.perf_counter()
+                batches[n].init()
+                batches[n].run()
+                sim_s += time.perf_counter() - t1
+                simulated += n * m.R
+                # Likelihood of each passing chain from its handles (chains may not be contiguous).
+                for j, c in enumerate(passed):
+                    m.calc_log_likelihood(sims[j * m.R:(j + 1) * m.R], int(c), int(c) + 1)
+            m.next_step(it, screened=True)
+            if on_iter:
+                on_iter(it)
+    finally:
+        for b in batches.values():
+            b.close()
+    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": simulated}
+
+
+def ess(samples: np.ndarray) -> np.ndarray:
+    """Multi-chain effective sample size per parameter (rank-free split-chain estimator of
+    Gelman et al., BDA3 11.5, with Geyer's initial monotone sequence). samples: (iters, chains, D)."""
+    n, m_, D = samples.shape
+    if n < 4:
+        return np.zeros(D)
+    half = n // 2
+    x = np.concatenate([samples[:half], samples[half:2 * half]], axis=1)  # split chains
+    n, m2 = x.shape[0], x.shape[1]
+    out = np.zeros(D)
+    for d in range(D):
+        y = x[:, :, d]
+        mean_c = y.mean(0)
+        var_c = y.var(0, ddof=1)
+        W = var_c.mean()
+        B = n * mean_c.var(ddof=1)
+        var_plus = (n - 1) / n * W + B / n
+        if not var_plus > 0:
+            out[d] = 0.0
+            continue
+        yc = y - mean_c
+        f = np.fft.rfft(yc, n=2 * n, axis=0)
+        acov = np.fft.irfft(f * np.conj(f), axis=0)[:n] / n  # per chain
+        rho = 1.0 - (W - acov.mean(1)) / var_plus
+        rho[0] = 1.0
+        # Geyer: sum pairs while positive, monotone.
+        tau, prev = -1.0, np.inf
+        for t in range(0, n - 1, 2):
+            pair = rho[t] + rho[t + 1]
+            if pair < 0:
+                break
+            pair = min(pair, prev)
+            prev = pair
+            tau += 2 * pair
+        out[d] = m2 * n / max(tau, 1e-12)
+    return out

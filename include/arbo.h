@@ -260,6 +260,13 @@ int arbo_sim_destroy(arbo_sim* s);
  * h_mExpectedPopSize of cpp/simulation.cpp:84-132. Values above mSize are capped. */
 int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* expected, size_t n);
 
+/* Changes the parameters of an existing handle between runs, as MCMC::copyParams does before each
+ * proposal's simulations (cpp/MCMC.cpp:75-82, cpp/main.cpp:96): transmission, dispersal, seeding,
+ * recovery and latency, seasonal expected-mosquito and attempt parameters. Sizes, life
+ * expectancies and table ranges must stay as created (ARBO_ERR_INVALID otherwise). Synchronises
+ * the device; takes effect at the next arbo_sim_init / step (batches pick it up as well). */
+int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p);
+
 /* Re-seed the handle (next arbo_sim_init uses it). */
 int arbo_sim_set_seed(arbo_sim* s, uint64_t seed, uint32_t instance);
 
@@ -395,6 +402,63 @@ int arbo_batch_autotune(arbo_batch* b, uint32_t steps_per_candidate, arbo_arch_p
 /* Measurement, as arbo_sim_time_phases / arbo_sim_time_steps for the whole batch. */
 int arbo_batch_time_phases(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* ms_out, void* stream);
 int arbo_batch_time_steps(arbo_batch* b, uint32_t nsteps, uint32_t flush_mb, float* step_ms, void* stream);
+
+/* ------------------------------------------------------------------ MCMC */
+
+/* Metropolis-Hastings chains whose likelihood comes from simulations (the MCMC class,
+ * cpp/MCMC.h:17-75, cpp/MCMC.cpp). Proposals, the negative-binomial log-likelihood of observed
+ * monthly cases and the acceptance test run in double precision on the GPU; every random number is
+ * keyed Philox of (seed, chain, iteration), so a serial program can replay a chain. The driver
+ * (host) sets each chain's proposal on its simulation handles (arbo_sim_set_param), runs them
+ * (alone or as a batch) and calls arbo_mcmc_loglik and arbo_mcmc_accept. */
+typedef struct arbo_mcmc arbo_mcmc;
+
+typedef struct arbo_mcmc_config {
+    uint32_t chains;       /* independent chains */
+    uint32_t params;       /* parameters per chain (<= 32) */
+    uint32_t replicates;   /* simulations per proposal, combined by log-mean-exp (cpp/MCMC.cpp:246-276); 0 = 1 */
+    uint32_t months;       /* observation periods */
+    uint32_t serotypes;    /* observed series per period */
+    uint32_t max_iters;    /* chain history kept on the device */
+    uint32_t report_param; /* index of the reporting rate: mean cases = rate * simulated cases */
+    uint32_t reserved;
+    const double* lo;      /* [params] prior box (uniform prior) */
+    const double* hi;      /* [params] */
+    const double* step;    /* [params] random-walk standard deviations */
+    const uint32_t* observed;    /* [months * serotypes] observed cases, month-major */
+    const uint32_t* month_start; /* [months + 1] first row of each period in the daily incidence series
+                                    (row t+1 holds step t), last entry = end */
+    double nb_size;        /* negative-binomial size (1 / dispersion of cpp/MCMC.cpp:236) */
+    uint64_t seed;
+} arbo_mcmc_config;
+
+int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out);
+int arbo_mcmc_destroy(arbo_mcmc* m);
+/* Current state of every chain (chains * params doubles); also loaded as the proposals so that
+ * arbo_mcmc_loglik(..., current = 1) can evaluate it, and recorded as iteration 0. */
+int arbo_mcmc_set_state(arbo_mcmc* m, const double* theta, void* stream);
+/* MCMC::propose (cpp/MCMC.cpp:100-137) without the adaptive covariance: theta + step * N(0, 1)
+ * per parameter. out (optional, chains * params) receives the proposals. */
+int arbo_mcmc_propose(arbo_mcmc* m, uint32_t iter, double* out, void* stream);
+/* MCMC::calcLogLikelihood (cpp/MCMC.cpp:218-276) for chains [c0, c1): sims holds (c1-c0)*replicates
+ * handles, row (c-c0)*replicates + r, that have just simulated the proposal (current = 0) or the
+ * current state (current = 1, which sets the chain's log posterior). */
+int arbo_mcmc_loglik(arbo_mcmc* m, arbo_sim* const* sims, uint32_t c0, uint32_t c1, int current, void* stream);
+/* MCMC::nextStep / reject (cpp/MCMC.cpp:278-365) for chains [c0, c1) at iteration iter; records the
+ * chain's state. screened = 1: delayed acceptance, second stage (see arbo_mcmc_screen). */
+int arbo_mcmc_accept(arbo_mcmc* m, uint32_t iter, uint32_t c0, uint32_t c1, int screened, void* stream);
+/* Delayed acceptance, first stage: screen_prop / screen_cur (chains doubles, screen_cur optional)
+ * are a cheap approximation of the log-likelihood of the proposals and of the current states;
+ * arbo_mcmc_screen then passes each proposal with probability min(1, exp(screen_prop - screen_cur))
+ * (pass, optional: chains bytes). No reference counterpart: the reference has no surrogate. */
+int arbo_mcmc_set_screen(arbo_mcmc* m, const double* screen_prop, const double* screen_cur, void* stream);
+int arbo_mcmc_screen(arbo_mcmc* m, uint32_t iter, uint8_t* pass, void* stream);
+/* Host copies (each optional): current states, log posteriors, last proposal log-likelihoods,
+ * accepted and first-stage-passed counts. */
+int arbo_mcmc_state(arbo_mcmc* m, double* theta, double* logpost, double* loglik, uint32_t* accepted,
+                    uint32_t* passed);
+/* Recorded states of the first iters iterations ([iter][chain][param]) and accept flags. */
+int arbo_mcmc_chain(arbo_mcmc* m, uint32_t iters, double* out, uint8_t* flags);
 
 /* ------------------------------------------------------------------ self-tests */
 

@@ -1,0 +1,56 @@
+"""MCMC host logic on CPU: the negative-binomial log-likelihood restatement, the period
+boundaries, the effective-sample-size estimator and the serial chain replay."""
+import math
+
+import numpy as np
+import pytest
+
+from arbo_gpu_fit_gb300 import configs
+from arbo_gpu_fit_gb300.mcmc import ess, month_rows, monthly, sim_seed
+from oracle import mcmc_serial
+
+
+def test_nb_logpmf_matches_scipy():
+    stats = pytest.importorskip("scipy.stats")
+    for k, r, mu in [(0, 10.0, 0.5), (3, 10.0, 2.5), (250, 10.0, 180.0), (17, 0.5, 3.0), (1000, 10.0, 1.0)]:
+        want = stats.nbinom.logpmf(k, r, r / (r + mu))
+        assert mcmc_serial.nb_logpmf(k, r, mu) == pytest.approx(max(-250.0, want), rel=1e-12, abs=1e-12)
+    assert mcmc_serial.nb_logpmf(0, 10.0, 0.0) == 0.0
+    assert mcmc_serial.nb_logpmf(4, 10.0, 0.0) == -250.0  # floored as cpp/MCMC.cpp:238-241 floors it
+
+
+def test_month_rows_cover_every_step_once():
+    rows = month_rows(3650, 120)
+    assert rows[0] == 1 and rows[-1] == 3651 and np.all(np.diff(rows) >= 30) and np.all(np.diff(rows) <= 31)
+    daily = np.arange(3651 * 4, dtype=np.uint32).reshape(3651, 4)
+    assert np.array_equal(monthly(daily, rows).sum(0), daily[1:].astype(np.int64).sum(0))
+
+
+def test_ess_of_ar1_chains():
+    rng = np.random.default_rng(0)
+    n, chains, phi = 4000, 8, 0.8
+    x = np.zeros((n, chains, 2))
+    for t in range(1, n):
+        x[t] = phi * x[t - 1] + rng.standard_normal((chains, 2))
+    got = ess(x)
+    want = n * chains * (1 - phi) / (1 + phi)
+    assert np.all(np.abs(got / want - 1) < 0.25), (got, want)
+    iid = ess(rng.standard_normal((n, chains, 1)))
+    assert abs(iid[0] / (n * chains) - 1) < 0.15
+
+
+def test_sim_seed_distinct():
+    seeds = {sim_seed(7, c, r, it) for c in range(8) for r in range(3) for it in range(50)}
+    assert len(seeds) == 8 * 3 * 50
+
+
+def test_serial_replay_is_deterministic_and_moves():
+    w = configs.scaled(600, 1800, 3, 60, seed=5, sigma=0.3, bitingRate=0.9, nInitialInf=20.0, mInitialInf=60.0)
+    obs = np.random.default_rng(1).integers(0, 30, (2, 4)).astype(np.uint32)
+    step = np.array([0.05, 0.05, 0.03, 0.05, 10.0, 0.02])
+    theta0 = np.array([[0.5, 0.5, 0.9, 0.5, 100.0, 0.2], [0.3, 0.7, 0.8, 0.2, 200.0, 0.1]])
+    a = mcmc_serial.run(w, obs, 2, step, 11, 5, theta0)
+    b = mcmc_serial.run(w, obs, 2, step, 11, 5, theta0)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.all(np.isfinite(a[2]))
+    assert np.all(a[0][0] == theta0)
