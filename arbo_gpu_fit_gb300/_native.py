@@ -109,6 +109,15 @@ SIGNATURES = {
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
     "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
     "arbo_sim_set_param": (c_int, [c_void_p, POINTER(SimParamStruct)]),
+    "arbo_mlp_create": (c_int, [c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_uint64, POINTER(c_void_p)]),
+    "arbo_mlp_destroy": (c_int, [c_void_p]),
+    "arbo_mlp_dims": (c_int, [c_void_p, POINTER(c_uint32), POINTER(c_uint32)]),
+    "arbo_mlp_forward": (c_int, [c_void_p, POINTER(c_float), c_uint32, POINTER(c_float), c_void_p]),
+    "arbo_mlp_gradients": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float), c_uint32, POINTER(c_float), c_void_p]),
+    "arbo_mlp_train_step": (c_int, [c_void_p, POINTER(c_float), POINTER(c_float), c_uint32, c_float, POINTER(c_float), c_void_p]),
+    "arbo_mlp_get_layer": (c_int, [c_void_p, c_uint32, POINTER(c_float), POINTER(c_float), POINTER(c_float), POINTER(c_float)]),
+    "arbo_mlp_set_layer": (c_int, [c_void_p, c_uint32, POINTER(c_float), POINTER(c_float)]),
+    "arbo_tc_gemm": (c_int, [POINTER(c_float), POINTER(c_float), c_uint32, c_uint32, c_uint32, POINTER(c_float), c_uint32, POINTER(c_float)]),
     "arbo_mcmc_create": (c_int, [POINTER(McmcConfigStruct), POINTER(c_void_p)]),
     "arbo_mcmc_destroy": (c_int, [c_void_p]),
     "arbo_mcmc_set_state": (c_int, [c_void_p, POINTER(ctypes.c_double), c_void_p]),

@@ -19,8 +19,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "libarbo_gb300.so"
-SOURCES = ["kernels.cu", "api.cu", "mcmc.cu", "selftest.cu"]
-HEADERS = ["philox.cuh", "sim_internal.h"]
+SOURCES = ["kernels.cu", "api.cu", "mcmc.cu", "mlp.cu", "selftest.cu"]
+HEADERS = ["philox.cuh", "sim_internal.h", "tc.cuh"]
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

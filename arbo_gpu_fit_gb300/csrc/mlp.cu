@@ -1,0 +1,580 @@
+// mlp.cu — the learned surrogate of the simulator: a multilayer perceptron (SiLU hidden layers)
+// trained on the GPU with BF16 operands and FP32 accumulation. Every matrix product runs on the
+// fifth-generation tensor cores (tcgen05.mma into tensor memory, tc.cuh); the epilogues fuse bias,
+// activation, activation derivative and the transposed copies the next products need; Adam updates
+// FP32 master weights and writes the BF16 copies. No reference counterpart: the reference has no
+// surrogate (include/arbo.h, section "surrogate").
+//
+// Products, all C = A * B^T with K-major BF16 operands (row-major A [M][K], B [N][K]):
+//   forward  Z_l  = H_{l-1} W_l^T          A = H_{l-1} [B][in],  B = W_l  [out][in]
+//   backward dH   = dZ_l W_l               A = dZ_l    [B][out], B = W_l^T [in][out]
+//   weights  dW_l = dZ_l^T H_{l-1}         A = dZ_l^T  [out][B], B = H_{l-1}^T [in][B]
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/arbo.h"
+#include "philox.cuh"
+#include "sim_internal.h"
+#include "tc.cuh"
+
+using namespace arbo;
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+enum Epi : int { kEpiHidden = 0, kEpiLinear = 1, kEpiBackward = 2, kEpiStore = 3 };
+
+struct GemmArgs {
+    const bf16* A;
+    const bf16* B;
+    uint32_t lda, ldb, M, N, K;
+    int epi;
+    const float* bias;   // [N]
+    const float* zprev;  // [M][ldz] pre-activation whose derivative scales the product (backward)
+    uint32_t ldz;
+    float* outf;         // [M][ldof]
+    uint32_t ldof;
+    bf16* outb;          // [M][ldob]
+    uint32_t ldob;
+    bf16* outt;          // [N][ldot] transposed copy
+    uint32_t ldot;
+    uint32_t* err;       // bit 0: an mbarrier wait ran out
+};
+
+constexpr uint32_t kTileM = 128, kTileN = 128, kTileK = 64;
+constexpr uint32_t kOperandBytes = kTileM * kTileK * 2;  // one operand chunk (16 KB)
+// Dynamic shared memory per CTA: the two operand chunks, padded so that at most four CTAs share an
+// SM and their 128-column accumulators fit the 512 tensor-memory columns without waiting.
+constexpr uint32_t kGemmSmem = 56 * 1024;
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
+__device__ __forceinline__ float dsilu(float z)
+{
+    const float s = 1.0f / (1.0f + expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+// One 128 x 128 output tile per CTA of 128 threads. The K loop stages 64-wide chunks of both
+// operands in the core-matrix layout, one thread issues four K=16 tensor-core products per chunk
+// and commits them to an mbarrier; every thread waits (bounded) before the chunk is overwritten.
+// The epilogue reads the accumulator from tensor memory, one row per thread.
+__global__ void __launch_bounds__(128, 1) k_gemm_tn(GemmArgs g)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ unsigned long long bar;
+    __shared__ uint32_t tmem_slot;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t m0 = blockIdx.x * kTileM, n0 = blockIdx.y * kTileN;
+    const uint32_t nt = min(kTileN, g.N - n0);
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kOperandBytes;
+    if (warp == 0) tc_alloc(&tmem_slot, kTileN);
+    if (tid == 0) tc_bar_init(&bar, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = tc_idesc_bf16(kTileM, nt);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t k0 = 0; k0 < g.K && ok; k0 += kTileK) {
+        for (uint32_t p = tid; p < kTileM * 8; p += blockDim.x) {
+            const uint32_t r = p >> 3, kb = p & 7u, k = k0 + kb * 8;
+            const uint32_t off = (r >> 3) * 1024 + kb * 128 + (r & 7u) * 16;
+            uint4 va = make_uint4(0, 0, 0, 0), vb = va;
+            if (m0 + r < g.M && k < g.K) va = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k);
+            if (n0 + r < g.N && k < g.K) vb = *reinterpret_cast<const uint4*>(g.B + (size_t)(n0 + r) * g.ldb + k);
+            *reinterpret_cast<uint4*>(sA + off) = va;
+            *reinterpret_cast<uint4*>(sB + off) = vb;
+        }
+        tc_fence_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t ks = min(4u, (g.K - k0) / 16);
+            for (uint32_t kk = 0; kk < ks; ++kk) {
+                const uint64_t ad = tc_desc(tc_smem(sA) + kk * 256, 128, 1024);
+                const uint64_t bd = tc_desc(tc_smem(sB) + kk * 256, 128, 1024);
+                tc_mma(tmem, ad, bd, idesc, k0 > 0 || kk > 0);
+            }
+            tc_commit(&bar);
+        }
+        ok = tc_bar_wait(&bar, phase);
+        phase ^= 1u;
+        ok = __syncthreads_and(ok);
+    }
+    tc_fence_after();
+    if (!ok) {
+        if (tid == 0) atomicOr(g.err, 1u);
+        tc_bar_wait(&bar, phase ^ 1u);  // bounded: whatever is still in flight
+    } else {
+        const uint32_t row = m0 + warp * 32 + lane;
+        const bool live = row < g.M;
+        for (uint32_t c0 = 0; c0 < nt; c0 += 16) {
+            float v[16];
+            tc_ld16(tmem + ((warp * 32u) << 16) + c0, v);
+            if (!live) continue;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const uint32_t n = n0 + c0 + j;
+                float x = v[j];
+                if (g.epi == kEpiHidden) {
+                    x += g.bias[n];
+                    g.outf[(size_t)row * g.ldof + n] = x;
+                    const bf16 h = __float2bfloat16_rn(silu(x));
+                    g.outb[(size_t)row * g.ldob + n] = h;
+                    g.outt[(size_t)n * g.ldot + row] = h;
+                } else if (g.epi == kEpiLinear) {
+                    g.outf[(size_t)row * g.ldof + n] = x + g.bias[n];
+                } else if (g.epi == kEpiBackward) {
+                    const bf16 dz = __float2bfloat16_rn(x * dsilu(g.zprev[(size_t)row * g.ldz + n]));
+                    g.outb[(size_t)row * g.ldob + n] = dz;
+                    g.outt[(size_t)n * g.ldot + row] = dz;
+                } else {
+                    g.outf[(size_t)row * g.ldof + n] = x;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, kTileN);
+}
+
+// Inputs: FP32 [n][nin] -> BF16 [n][ldx] (zero padded) and transposed [ldx][ldt].
+__global__ void k_stage_input(const float* __restrict__ x, uint32_t n, uint32_t nin, uint32_t ldx, bf16* xb, bf16* xt,
+                              uint32_t ldt)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * ldx) return;
+    const uint32_t r = i / ldx, c = i - r * ldx;
+    const bf16 v = __float2bfloat16_rn(c < nin ? x[(size_t)r * nin + c] : 0.0f);
+    xb[i] = v;
+    xt[(size_t)c * ldt + r] = v;
+}
+
+// Mean squared error over the real outputs and its gradient dL/dY = 2 (Y - T) / (n * nout).
+__global__ void k_loss(const float* __restrict__ y, const float* __restrict__ t, uint32_t n, uint32_t nout,
+                       uint32_t ldy, bf16* dy, bf16* dyt, uint32_t ldt, float* loss)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float e2 = 0.0f;
+    if (i < n * ldy) {
+        const uint32_t r = i / ldy, c = i - r * ldy;
+        float g = 0.0f;
+        if (c < nout) {
+            const float e = y[(size_t)r * ldy + c] - t[(size_t)r * nout + c];
+            e2 = e * e;
+            g = 2.0f * e / (float)(n * nout);
+        }
+        const bf16 gb = __float2bfloat16_rn(g);
+        dy[(size_t)r * ldy + c] = gb;
+        dyt[(size_t)c * ldt + r] = gb;
+    }
+    for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+    if ((threadIdx.x & 31u) == 0 && e2 != 0.0f) atomicAdd(loss, e2 / (float)(n * nout));
+}
+
+// Bias gradient: db[c] = sum over rows of dZ, from the transposed copy (one warp per column).
+__global__ void k_bias_grad(const bf16* __restrict__ dzt, uint32_t ldt, uint32_t n, uint32_t cols, float* db)
+{
+    const uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+    if (c >= cols) return;
+    float s = 0.0f;
+    for (uint32_t r = lane; r < n; r += 32) s += __bfloat162float(dzt[(size_t)c * ldt + r]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) db[c] = s;
+}
+
+// Adam (Kingma & Ba 2015) on FP32 master weights; writes the BF16 copy and its transpose.
+__global__ void k_adam(float* w, float* m, float* v, const float* __restrict__ g, uint32_t count, uint32_t rows,
+                       uint32_t cols, bf16* wb, bf16* wt, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) {
+        const uint32_t r = i / cols, c = i - r * cols;
+        const bf16 b = __float2bfloat16_rn(wi);
+        wb[i] = b;
+        wt[(size_t)c * rows + r] = b;
+    }
+}
+
+__global__ void k_cast_weights(const float* __restrict__ w, uint32_t rows, uint32_t cols, bf16* wb, bf16* wt)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    const uint32_t r = i / cols, c = i - r * cols;
+    const bf16 b = __float2bfloat16_rn(w[i]);
+    wb[i] = b;
+    wt[(size_t)c * rows + r] = b;
+}
+
+int ufail(int code, const std::string& msg) { return set_error(code, msg); }
+
+#define UCUDA(expr)                                                                                     \
+    do {                                                                                                \
+        cudaError_t e_ = (expr);                                                                        \
+        if (e_ != cudaSuccess) return ufail(ARBO_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+uint32_t up16(uint32_t x) { return (x + 15u) & ~15u; }
+
+}  // namespace
+
+struct arbo_mlp {
+    int device = 0;
+    uint32_t L = 0;                    // linear layers
+    std::vector<uint32_t> dim;         // padded widths, dim[0] = input, dim[L] = output
+    uint32_t nin = 0, nout = 0, maxb = 0;
+    std::vector<float*> w, b, mw, vw, mb, vb, dw, db;
+    std::vector<bf16*> wb, wt;
+    bf16 *x = nullptr, *xt = nullptr;
+    std::vector<float*> z;             // pre-activations of hidden layers [maxb][dim]
+    std::vector<bf16*> h, ht;          // activations of hidden layers
+    float* y = nullptr;                // outputs [maxb][dim[L]]
+    bf16 *d0 = nullptr, *d0t = nullptr, *d1 = nullptr, *d1t = nullptr;  // ping-pong dZ and transposes
+    float *xin = nullptr, *tin = nullptr, *loss = nullptr;
+    uint32_t* err = nullptr;
+    uint32_t steps = 0;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+int mlp_gemm(arbo_mlp* n, const bf16* A, uint32_t lda, const bf16* B, uint32_t ldb, uint32_t M, uint32_t N,
+             uint32_t K, int epi, const float* bias, const float* zprev, uint32_t ldz, float* outf, uint32_t ldof,
+             bf16* outb, uint32_t ldob, bf16* outt, uint32_t ldot, cudaStream_t st)
+{
+    GemmArgs g{A, B, lda, ldb, M, N, K, epi, bias, zprev, ldz, outf, ldof, outb, ldob, outt, ldot, n->err};
+    const dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
+    k_gemm_tn<<<grid, 128, kGemmSmem, st>>>(g);
+    return (int)cudaGetLastError();
+}
+
+int mlp_forward(arbo_mlp* n, uint32_t rows, cudaStream_t st)
+{
+    const uint32_t ld = n->maxb;
+    k_stage_input<<<(rows * n->dim[0] + 255) / 256, 256, 0, st>>>(n->xin, rows, n->nin, n->dim[0], n->x, n->xt, ld);
+    const bf16* a = n->x;
+    for (uint32_t l = 0; l < n->L; ++l) {
+        const uint32_t in = n->dim[l], out = n->dim[l + 1];
+        int e;
+        if (l + 1 < n->L)
+            e = mlp_gemm(n, a, in, n->wb[l], in, rows, out, in, kEpiHidden, n->b[l], nullptr, 0, n->z[l], out, n->h[l],
+                         out, n->ht[l], ld, st);
+        else
+            e = mlp_gemm(n, a, in, n->wb[l], in, rows, out, in, kEpiLinear, n->b[l], nullptr, 0, n->y, out, nullptr, 0,
+                         nullptr, 0, st);
+        if (e) return e;
+        if (l + 1 < n->L) a = n->h[l];
+    }
+    return 0;
+}
+
+int mlp_backward(arbo_mlp* n, uint32_t rows, cudaStream_t st)
+{
+    const uint32_t ld = n->maxb, L = n->L;
+    cudaMemsetAsync(n->loss, 0, 4, st);
+    const uint32_t outw = n->dim[L];
+    k_loss<<<(rows * outw + 255) / 256, 256, 0, st>>>(n->y, n->tin, rows, n->nout, outw, n->d0, n->d0t, ld, n->loss);
+    bf16 *dz = n->d0, *dzt = n->d0t, *nd = n->d1, *ndt = n->d1t;
+    for (uint32_t l = L; l-- > 0;) {
+        const uint32_t in = n->dim[l], out = n->dim[l + 1];
+        const bf16* hprevt = l == 0 ? n->xt : n->ht[l - 1];
+        // dW_l = dZ^T H_{l-1}: M = out, N = in, K = rows.
+        int e = mlp_gemm(n, dzt, ld, hprevt, ld, out, in, rows, kEpiStore, nullptr, nullptr, 0, n->dw[l], in, nullptr,
+                         0, nullptr, 0, st);
+        if (e) return e;
+        k_bias_grad<<<(out + 7) / 8, 256, 0, st>>>(dzt, ld, rows, out, n->db[l]);
+        if (l > 0) {
+            // dZ_{l-1} = (dZ_l W_l) * silu'(Z_{l-1}): M = rows, N = in, K = out.
+            e = mlp_gemm(n, dz, out, n->wt[l], out, rows, in, out, kEpiBackward, nullptr, n->z[l - 1], in, nullptr, 0,
+                         nd, in, ndt, ld, st);
+            if (e) return e;
+            std::swap(dz, nd);
+            std::swap(dzt, ndt);
+        }
+    }
+    return (int)cudaGetLastError();
+}
+
+int mlp_upload(arbo_mlp* n, const float* x, const float* t, uint32_t rows, cudaStream_t st)
+{
+    if (rows == 0 || rows > n->maxb || rows % 16) return ufail(ARBO_ERR_INVALID, "batch rows must be a multiple of 16 in [16, max_batch]");
+    UCUDA(cudaMemcpyAsync(n->xin, x, (size_t)rows * n->nin * 4, cudaMemcpyHostToDevice, st));
+    if (t) UCUDA(cudaMemcpyAsync(n->tin, t, (size_t)rows * n->nout * 4, cudaMemcpyHostToDevice, st));
+    return ARBO_OK;
+}
+
+int mlp_check_err(arbo_mlp* n, cudaStream_t st)
+{
+    uint32_t e = 0;
+    UCUDA(cudaMemcpyAsync(&e, n->err, 4, cudaMemcpyDeviceToHost, st));
+    UCUDA(cudaStreamSynchronize(st));
+    if (e) return ufail(ARBO_ERR_CUDA, "tensor-core product: an mbarrier wait ran out (error word " + std::to_string(e) + ")");
+    return ARBO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int arbo_mlp_create(uint32_t n_in, uint32_t hidden, uint32_t hidden_layers, uint32_t n_out, uint32_t max_batch,
+                    uint64_t seed, arbo_mlp** out)
+{
+    if (!out || n_in == 0 || n_in > 4096 || hidden == 0 || hidden % 16 || hidden > 8192 || hidden_layers == 0 ||
+        n_out == 0 || n_out > 8192 || max_batch == 0 || max_batch % 16 || max_batch > (1u << 16))
+        return ufail(ARBO_ERR_INVALID, "arbo_mlp_create: hidden and max_batch multiples of 16; sizes within limits");
+    *out = nullptr;
+    arbo_mlp* n = new arbo_mlp();
+    UCUDA(cudaGetDevice(&n->device));
+    static bool attr = false;
+    if (!attr) {
+        UCUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
+        attr = true;
+    }
+    n->L = hidden_layers + 1;
+    n->nin = n_in;
+    n->nout = n_out;
+    n->maxb = max_batch;
+    n->dim.push_back(up16(n_in));
+    for (uint32_t l = 0; l < hidden_layers; ++l) n->dim.push_back(hidden);
+    n->dim.push_back(up16(n_out));
+    auto alloc = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, bytes ? bytes : 16);
+        n->allocs.push_back(p);
+        return p;
+    };
+    bool okm = true;
+    auto F = [&](size_t cnt) {
+        float* p = (float*)alloc(cnt * 4);
+        okm = okm && p;
+        return p;
+    };
+    auto H = [&](size_t cnt) {
+        bf16* p = (bf16*)alloc(cnt * 2);
+        okm = okm && p;
+        return p;
+    };
+    std::vector<float> hw;
+    for (uint32_t l = 0; l < n->L; ++l) {
+        const uint32_t in = n->dim[l], o = n->dim[l + 1];
+        const size_t cnt = (size_t)in * o;
+        n->w.push_back(F(cnt));
+        n->mw.push_back(F(cnt));
+        n->vw.push_back(F(cnt));
+        n->dw.push_back(F(cnt));
+        n->b.push_back(F(o));
+        n->mb.push_back(F(o));
+        n->vb.push_back(F(o));
+        n->db.push_back(F(o));
+        n->wb.push_back(H(cnt));
+        n->wt.push_back(H(cnt));
+        if (!okm) break;
+        // Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from the keyed stream; padded inputs and outputs
+        // have zero weights.
+        const uint32_t fan = l == 0 ? n_in : n->dim[l];
+        const float bound = 1.0f / std::sqrt((float)fan);
+        const uint32_t ro = (l + 1 == n->L) ? n_out : o, ri = l == 0 ? n_in : in;
+        hw.assign(cnt, 0.0f);
+        const Key key{(uint32_t)seed, (uint32_t)(seed >> 32), 0};
+        for (uint32_t r = 0; r < ro; ++r)
+            for (uint32_t c = 0; c < ri; c += 4) {
+                const U4 u = draw4(key, 0x3Fu, l, r, c);
+                for (uint32_t q = 0; q < 4 && c + q < ri; ++q) hw[(size_t)r * in + c + q] = (2.0f * u01(u.v[q]) - 1.0f) * bound;
+            }
+        UCUDA(cudaMemcpy(n->w[l], hw.data(), cnt * 4, cudaMemcpyHostToDevice));
+        k_cast_weights<<<(uint32_t)((cnt + 255) / 256), 256>>>(n->w[l], o, in, n->wb[l], n->wt[l]);
+    }
+    const uint32_t B = max_batch;
+    n->x = H((size_t)B * n->dim[0]);
+    n->xt = H((size_t)B * n->dim[0]);
+    uint32_t widest = 0;
+    for (uint32_t d : n->dim) widest = std::max(widest, d);
+    for (uint32_t l = 0; l + 1 < n->L; ++l) {
+        n->z.push_back(F((size_t)B * n->dim[l + 1]));
+        n->h.push_back(H((size_t)B * n->dim[l + 1]));
+        n->ht.push_back(H((size_t)B * n->dim[l + 1]));
+    }
+    n->y = F((size_t)B * n->dim[n->L]);
+    n->d0 = H((size_t)B * widest);
+    n->d0t = H((size_t)B * widest);
+    n->d1 = H((size_t)B * widest);
+    n->d1t = H((size_t)B * widest);
+    n->xin = F((size_t)B * n_in);
+    n->tin = F((size_t)B * n_out);
+    n->loss = F(1);
+    n->err = (uint32_t*)alloc(4);
+    if (!okm || !n->err) {
+        arbo_mlp_destroy(n);
+        return ufail(ARBO_ERR_ALLOC, "arbo_mlp_create: device allocation failed");
+    }
+    UCUDA(cudaDeviceSynchronize());
+    *out = n;
+    return ARBO_OK;
+}
+
+int arbo_mlp_destroy(arbo_mlp* n)
+{
+    if (!n) return ARBO_OK;
+    cudaSetDevice(n->device);
+    for (void* p : n->allocs) cudaFree(p);
+    delete n;
+    return ARBO_OK;
+}
+
+int arbo_mlp_dims(const arbo_mlp* n, uint32_t* layers, uint32_t* dims)
+{
+    if (!n) return ufail(ARBO_ERR_INVALID, "null network");
+    if (layers) *layers = n->L;
+    if (dims)
+        for (uint32_t l = 0; l <= n->L; ++l) dims[l] = n->dim[l];
+    return ARBO_OK;
+}
+
+int arbo_mlp_forward(arbo_mlp* n, const float* x, uint32_t rows, float* y, void* stream)
+{
+    if (!n || !x || !y) return ufail(ARBO_ERR_INVALID, "null argument");
+    UCUDA(cudaSetDevice(n->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = mlp_upload(n, x, nullptr, rows, st);
+    if (e) return e;
+    if ((e = mlp_forward(n, rows, st))) return ufail(ARBO_ERR_CUDA, std::string("forward: ") + cudaGetErrorString((cudaError_t)e));
+    const uint32_t w = n->dim[n->L];
+    if (w == n->nout) {
+        UCUDA(cudaMemcpyAsync(y, n->y, (size_t)rows * w * 4, cudaMemcpyDeviceToHost, st));
+    } else {
+        UCUDA(cudaMemcpy2DAsync(y, n->nout * 4, n->y, w * 4, n->nout * 4, rows, cudaMemcpyDeviceToHost, st));
+    }
+    return mlp_check_err(n, st);
+}
+
+int arbo_mlp_gradients(arbo_mlp* n, const float* x, const float* t, uint32_t rows, float* loss, void* stream)
+{
+    if (!n || !x || !t) return ufail(ARBO_ERR_INVALID, "null argument");
+    UCUDA(cudaSetDevice(n->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    int e = mlp_upload(n, x, t, rows, st);
+    if (e) return e;
+    if ((e = mlp_forward(n, rows, st)) || (e = mlp_backward(n, rows, st)))
+        return ufail(ARBO_ERR_CUDA, std::string("forward/backward: ") + cudaGetErrorString((cudaError_t)e));
+    if (loss) UCUDA(cudaMemcpyAsync(loss, n->loss, 4, cudaMemcpyDeviceToHost, st));
+    return mlp_check_err(n, st);
+}
+
+int arbo_mlp_train_step(arbo_mlp* n, const float* x, const float* t, uint32_t rows, float lr, float* loss, void* stream)
+{
+    int e = arbo_mlp_gradients(n, x, t, rows, loss, stream);
+    if (e) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    n->steps += 1;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.0f - std::pow(b1, (float)n->steps), c2 = 1.0f - std::pow(b2, (float)n->steps);
+    for (uint32_t l = 0; l < n->L; ++l) {
+        const uint32_t in = n->dim[l], o = n->dim[l + 1], cnt = in * o;
+        k_adam<<<(cnt + 255) / 256, 256, 0, st>>>(n->w[l], n->mw[l], n->vw[l], n->dw[l], cnt, o, in, n->wb[l], n->wt[l],
+                                                  lr, b1, b2, eps, c1, c2);
+        k_adam<<<(o + 255) / 256, 256, 0, st>>>(n->b[l], n->mb[l], n->vb[l], n->db[l], o, 1, o, nullptr, nullptr, lr, b1,
+                                                b2, eps, c1, c2);
+    }
+    UCUDA(cudaGetLastError());
+    return ARBO_OK;
+}
+
+int arbo_mlp_get_layer(const arbo_mlp* n, uint32_t layer, float* w, float* b, float* dw, float* db)
+{
+    if (!n || layer >= n->L) return ufail(ARBO_ERR_INVALID, "bad layer");
+    UCUDA(cudaSetDevice(n->device));
+    UCUDA(cudaDeviceSynchronize());
+    const size_t cnt = (size_t)n->dim[layer] * n->dim[layer + 1], o = n->dim[layer + 1];
+    if (w) UCUDA(cudaMemcpy(w, n->w[layer], cnt * 4, cudaMemcpyDeviceToHost));
+    if (b) UCUDA(cudaMemcpy(b, n->b[layer], o * 4, cudaMemcpyDeviceToHost));
+    if (dw) UCUDA(cudaMemcpy(dw, n->dw[layer], cnt * 4, cudaMemcpyDeviceToHost));
+    if (db) UCUDA(cudaMemcpy(db, n->db[layer], o * 4, cudaMemcpyDeviceToHost));
+    return ARBO_OK;
+}
+
+int arbo_mlp_set_layer(arbo_mlp* n, uint32_t layer, const float* w, const float* b)
+{
+    if (!n || layer >= n->L) return ufail(ARBO_ERR_INVALID, "bad layer");
+    UCUDA(cudaSetDevice(n->device));
+    const uint32_t in = n->dim[layer], o = n->dim[layer + 1];
+    const size_t cnt = (size_t)in * o;
+    if (w) {
+        UCUDA(cudaMemcpy(n->w[layer], w, cnt * 4, cudaMemcpyHostToDevice));
+        k_cast_weights<<<(uint32_t)((cnt + 255) / 256), 256>>>(n->w[layer], o, in, n->wb[layer], n->wt[layer]);
+        UCUDA(cudaGetLastError());
+    }
+    if (b) UCUDA(cudaMemcpy(n->b[layer], b, o * 4, cudaMemcpyHostToDevice));
+    UCUDA(cudaDeviceSynchronize());
+    return ARBO_OK;
+}
+
+// One tensor-core product C = A B^T of BF16 inputs given as FP32 (rounded to BF16 here), FP32
+// result: exposes the GEMM kernel alone for checks and timing. A [M][K], B [N][K], C [M][N].
+int arbo_tc_gemm(const float* a, const float* b, uint32_t M, uint32_t N, uint32_t K, float* c, uint32_t reps,
+                 float* ms)
+{
+    if (!a || !b || !c || M == 0 || N == 0 || K == 0 || N % 16 || K % 16)
+        return ufail(ARBO_ERR_INVALID, "arbo_tc_gemm: N and K multiples of 16");
+    UCUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
+    std::vector<bf16> ha((size_t)M * K), hb((size_t)N * K);
+    for (size_t i = 0; i < ha.size(); ++i) ha[i] = __float2bfloat16_rn(a[i]);
+    for (size_t i = 0; i < hb.size(); ++i) hb[i] = __float2bfloat16_rn(b[i]);
+    bf16 *da = nullptr, *db = nullptr;
+    float* dc = nullptr;
+    uint32_t* derr = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(da);
+        cudaFree(db);
+        cudaFree(dc);
+        cudaFree(derr);
+    };
+    if (cudaMalloc(&da, ha.size() * 2) || cudaMalloc(&db, hb.size() * 2) || cudaMalloc(&dc, (size_t)M * N * 4) ||
+        cudaMalloc(&derr, 4)) {
+        cleanup();
+        return ufail(ARBO_ERR_ALLOC, "arbo_tc_gemm: allocation");
+    }
+    cudaMemcpy(da, ha.data(), ha.size() * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(db, hb.data(), hb.size() * 2, cudaMemcpyHostToDevice);
+    cudaMemset(derr, 0, 4);
+    GemmArgs g{da, db, K, K, M, N, K, kEpiStore, nullptr, nullptr, 0, dc, N, nullptr, 0, nullptr, 0, derr};
+    const dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_gemm_tn<<<grid, 128, kGemmSmem>>>(g);
+    cudaEventRecord(e0);
+    for (uint32_t r = 0; r < reps; ++r) k_gemm_tn<<<grid, 128, kGemmSmem>>>(g);
+    cudaEventRecord(e1);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = reps ? t / reps : 0.0f;
+    uint32_t herr = 0;
+    if (ce == cudaSuccess) ce = cudaMemcpy(c, dc, (size_t)M * N * 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    if (ce != cudaSuccess) return ufail(ARBO_ERR_CUDA, std::string("arbo_tc_gemm: ") + cudaGetErrorString(ce));
+    if (herr) return ufail(ARBO_ERR_CUDA, "arbo_tc_gemm: an mbarrier wait ran out");
+    return ARBO_OK;
+}
+
+}  // extern "C"

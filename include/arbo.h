@@ -460,6 +460,38 @@ int arbo_mcmc_state(arbo_mcmc* m, double* theta, double* logpost, double* loglik
 /* Recorded states of the first iters iterations ([iter][chain][param]) and accept flags. */
 int arbo_mcmc_chain(arbo_mcmc* m, uint32_t iters, double* out, uint8_t* flags);
 
+/* ------------------------------------------------------------------ surrogate */
+
+/* A multilayer perceptron (hidden_layers SiLU layers of `hidden` units, linear output) trained on
+ * the GPU as the first stage of delayed-acceptance MCMC: inputs are parameter vectors, outputs the
+ * simulator's (transformed) monthly incidence. Every matrix product runs on the tensor cores with
+ * BF16 operands and FP32 accumulation in tensor memory; bias, activation, activation derivative
+ * and Adam run fused or as element-wise kernels; weights are FP32 masters with BF16 copies. No
+ * reference counterpart: the reference has no surrogate. Widths are padded to multiples of 16;
+ * batches are multiples of 16 up to max_batch. Host buffers in and out. */
+typedef struct arbo_mlp arbo_mlp;
+
+int arbo_mlp_create(uint32_t n_in, uint32_t hidden, uint32_t hidden_layers, uint32_t n_out, uint32_t max_batch,
+                    uint64_t seed, arbo_mlp** out);
+int arbo_mlp_destroy(arbo_mlp* n);
+/* Number of linear layers and the padded widths (layers + 1 entries). */
+int arbo_mlp_dims(const arbo_mlp* n, uint32_t* layers, uint32_t* dims);
+/* y[rows][n_out] = network(x[rows][n_in]). */
+int arbo_mlp_forward(arbo_mlp* n, const float* x, uint32_t rows, float* y, void* stream);
+/* Forward and backward pass of the mean squared error against t[rows][n_out]; gradients are left
+ * on the device (arbo_mlp_get_layer), loss optional. */
+int arbo_mlp_gradients(arbo_mlp* n, const float* x, const float* t, uint32_t rows, float* loss, void* stream);
+/* arbo_mlp_gradients followed by one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) at rate lr. */
+int arbo_mlp_train_step(arbo_mlp* n, const float* x, const float* t, uint32_t rows, float lr, float* loss, void* stream);
+/* Host copies of layer `layer`: FP32 weights [out][in] (padded widths), biases, and the last
+ * gradients (each pointer optional); and the setter of weights and biases. */
+int arbo_mlp_get_layer(const arbo_mlp* n, uint32_t layer, float* w, float* b, float* dw, float* db);
+int arbo_mlp_set_layer(arbo_mlp* n, uint32_t layer, const float* w, const float* b);
+/* One tensor-core product c[M][N] = a[M][K] * b[N][K]^T with a and b rounded to BF16 and an FP32
+ * result, timed over reps launches (ms per launch, optional). N and K multiples of 16. */
+int arbo_tc_gemm(const float* a, const float* b, uint32_t M, uint32_t N, uint32_t K, float* c, uint32_t reps,
+                 float* ms);
+
 /* ------------------------------------------------------------------ self-tests */
 
 /* Evaluate the device Philox4x32-10 on n (counter[4], key[2]) records packed as 6 uint32 each
