@@ -121,6 +121,7 @@ SIGNATURES = {
     "arbo_mcmc_create": (c_int, [POINTER(McmcConfigStruct), POINTER(c_void_p)]),
     "arbo_mcmc_destroy": (c_int, [c_void_p]),
     "arbo_mcmc_set_state": (c_int, [c_void_p, POINTER(ctypes.c_double), c_void_p]),
+    "arbo_mcmc_set_step": (c_int, [c_void_p, POINTER(ctypes.c_double)]),
     "arbo_mcmc_propose": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_double), c_void_p]),
     "arbo_mcmc_loglik": (c_int, [c_void_p, POINTER(c_void_p), c_uint32, c_uint32, c_int, c_void_p]),
     "arbo_mcmc_accept": (c_int, [c_void_p, c_uint32, c_uint32, c_uint32, c_int, c_void_p]),

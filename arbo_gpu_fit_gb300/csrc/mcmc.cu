@@ -303,6 +303,15 @@ int arbo_mcmc_set_state(arbo_mcmc* h, const double* theta, void* stream)
     return cudaStreamSynchronize((cudaStream_t)stream) == cudaSuccess ? ARBO_OK : mfail(ARBO_ERR_CUDA, "sync");
 }
 
+int arbo_mcmc_set_step(arbo_mcmc* h, const double* step)
+{
+    if (!h || !step) return mfail(ARBO_ERR_INVALID, "null argument");
+    MCUDA(cudaSetDevice(h->device));
+    MCUDA(cudaDeviceSynchronize());
+    MCUDA(cudaMemcpy((void*)h->m.step, step, (size_t)h->m.D * 8, cudaMemcpyHostToDevice));
+    return ARBO_OK;
+}
+
 int arbo_mcmc_propose(arbo_mcmc* h, uint32_t iter, double* out, void* stream)
 {
     if (!h) return mfail(ARBO_ERR_INVALID, "null handle");

@@ -1,0 +1,151 @@
+"""The fit: synthetic reported cases from a seeded true parameter vector, then Metropolis-Hastings
+chains in two modes on the same GPU, compared by effective posterior samples per minute.
+
+* plain: one proposal at a time (run_plain), the reference's way of running its chain
+  (cpp/main.cpp:72-350), 64 chains one after another;
+* batched + surrogate: delayed acceptance (run_delayed) whose first stage is the tensor-core
+  surrogate trained on simulator runs of the same workload (surrogate.training_set), and whose
+  second stage simulates the passing proposals of all chains together in one batch.
+
+Observation model: monthly reported cases per serotype ~ NB(mean = reporting rate x simulated
+cases, size 10); uniform prior on the box of configs.PRIOR_BOX.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import configs, mcmc
+from .surrogate import Surrogate, training_set
+
+THETA_TRUE = np.array([0.5, 0.5, 0.9, 0.5, 100.0, 0.1])
+STEP_FRACTION = 0.04  # random-walk standard deviation as a fraction of the box width
+
+
+@dataclass
+class FitSetup:
+    workload: configs.Workload
+    observed: np.ndarray
+    theta0: np.ndarray
+    step: np.ndarray
+    chains: int
+    months: int
+    info: dict = field(default_factory=dict)
+
+
+def workload(population: str, seed: int = configs.DEFAULT_SEED) -> configs.Workload:
+    """'large': the config-1 population (1e6 humans, 6e6 slots, 50x50 communities) over 10 years;
+    'small': 1e4 humans, 6e4 slots, 10x10 communities over 10 years (same rates)."""
+    if population == "large":
+        return configs.plain_large(seed=seed, max_time=3650)
+    return configs.scaled(10_000, 60_000, 10, 3650, seed=seed)
+
+
+def setup(population: str = "small", chains: int = 64, months: int = 120, seed: int = 11,
+          start: str = "near") -> FitSetup:
+    """start 'near': chains start within 5 % of the box width of the true vector, so that the
+    comparison measures mixing rather than burn-in; 'spread': over the middle half of the box."""
+    w = workload(population)
+    obs = mcmc.synthetic_data(w, THETA_TRUE, months=months, seed=seed)
+    lo = np.array([b[1] for b in configs.PRIOR_BOX])
+    hi = np.array([b[2] for b in configs.PRIOR_BOX])
+    rng = np.random.default_rng(seed)
+    if start == "near":
+        theta0 = np.clip(THETA_TRUE + 0.05 * (hi - lo) * rng.uniform(-1, 1, (chains, len(lo))), lo, hi)
+    else:
+        theta0 = lo + (hi - lo) * rng.uniform(0.25, 0.75, (chains, len(lo)))
+    step = STEP_FRACTION * (hi - lo)
+    return FitSetup(w, obs, theta0, step, chains, months, {"population": population})
+
+
+def summarize(chain: np.ndarray, minutes: float, burn: int) -> dict:
+    """Posterior summary of recorded states [iters, chains, D] after discarding `burn` iterations."""
+    k = int(burn)
+    post = chain[k:]
+    e = mcmc.ess(post)
+    return {"iters": int(chain.shape[0]), "kept": int(post.shape[0]), "ess": e.tolist(), "ess_min": float(e.min()),
+            "minutes": minutes, "ess_per_min": float(e.min() / minutes) if minutes > 0 else None,
+            "mean": post.reshape(-1, post.shape[2]).mean(0).tolist()}
+
+
+def run_plain(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    r = mcmc.run_plain(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
+    chain, flags = m.chain(iters)
+    out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
+    out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
+               s_per_iter=r["wall_s"] / iters, chain=chain)
+    m.close()
+    return out
+
+
+def train_surrogate(fs: FitSetup, runs: int, epochs: int, seed: int = 3, hidden: int = 512, layers: int = 4,
+                    batch_size: int = 64, lr: float = 1e-3) -> tuple:
+    t0 = time.perf_counter()
+    theta, inc = training_set(fs.workload, runs, fs.months, seed=seed, batch_size=batch_size)
+    t1 = time.perf_counter()
+    sur = Surrogate(fs.months, fs.observed.shape[1], hidden=hidden, hidden_layers=layers, seed=seed)
+    losses = sur.fit(theta, inc, epochs, batch=256, lr=lr, seed=seed, decay=0.02)
+    t2 = time.perf_counter()
+    return sur, {"runs": runs, "epochs": epochs, "simulate_s": t1 - t0, "train_s": t2 - t1,
+                 "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
+
+
+def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    r = mcmc.run_delayed(m, iters, fs.theta0, lambda th: sur.loglik(th, fs.observed),
+                         adapt=mcmc.StepAdapter(adapt_until))
+    chain, flags = m.chain(iters)
+    st = m.state()
+    out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
+    out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
+               passed=float(st["passed"].sum() / (fs.chains * (iters - 1))), s_per_iter=r["wall_s"] / iters,
+               chain=chain)
+    m.close()
+    return out
+
+
+def run_batched(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    r = mcmc.run_batched(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
+    chain, flags = m.chain(iters)
+    out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
+    out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
+               s_per_iter=r["wall_s"] / iters, chain=chain)
+    m.close()
+    return out
+
+
+def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt_until: int = 60,
+            plain_iters: int = 20, train_runs: int = 4096, epochs: int = 60, seed: int = 11) -> dict:
+    """Plain, batched and batched + surrogate (delayed acceptance) chains on one setup.
+
+    Plain and batched produce bit-identical chains (the random streams are keyed; tested), so the
+    plain chain's effective sample size for `iters` iterations is the batched chain's, and its
+    time is plain_iters measured iterations scaled to `iters` (every iteration simulates every
+    chain once). The first plain_iters states of both are compared here as well."""
+    fs = setup(population, chains=chains, seed=seed)
+    out = {"population": population, "chains": chains, "iters": iters, "adapt_until": adapt_until,
+           "theta_true": THETA_TRUE.tolist()}
+    b = run_batched(fs, iters, adapt_until=adapt_until)
+    p = run_plain(fs, plain_iters, adapt_until=adapt_until)
+    same = bool(np.array_equal(p["chain"], b["chain"][:plain_iters]))
+    plain_minutes = p["s_per_iter"] * iters / 60.0
+    plain = {"s_per_iter": p["s_per_iter"], "measured_iters": plain_iters, "minutes_for_iters": plain_minutes,
+             "ess_min": b["ess_min"], "ess_per_min": b["ess_min"] / plain_minutes, "same_chain_as_batched": same}
+    sur, info = train_surrogate(fs, train_runs, epochs, seed=seed)
+    d = run_delayed(fs, sur, iters, adapt_until=adapt_until)
+    train_min = (info["simulate_s"] + info["train_s"]) / 60.0
+    for r_ in (b, d):
+        r_.pop("chain")
+    p.pop("chain")
+    out.update(plain=plain, batched=b, delayed=d, surrogate=info)
+    out["delayed"]["ess_per_min_incl_training"] = d["ess_min"] / (d["minutes"] + train_min)
+    out["speedup_batched_vs_plain"] = b["ess_per_min"] / plain["ess_per_min"]
+    out["speedup_delayed_vs_plain"] = d["ess_per_min"] / plain["ess_per_min"]
+    out["speedup_delayed_vs_plain_incl_training"] = out["delayed"]["ess_per_min_incl_training"] / plain["ess_per_min"]
+    mb, md = np.array(b["mean"]), np.array(d["mean"])
+    out["delayed_mean_rel_diff_vs_exact"] = (np.abs(md - mb) / np.abs(mb)).tolist()
+    return out

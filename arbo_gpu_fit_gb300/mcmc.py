@@ -112,6 +112,10 @@ class MCMC:
         t = np.ascontiguousarray(theta, np.float64).reshape(self.C, self.D)
         check(self._lib.arbo_mcmc_set_state(self._h, _dp(t), None))
 
+    def set_step(self, step) -> None:
+        self.step_sd = np.ascontiguousarray(step, np.float64)
+        check(self._lib.arbo_mcmc_set_step(self._h, _dp(self.step_sd)))
+
     def propose(self, it: int) -> np.ndarray:
         out = np.zeros((self.C, self.D), np.float64)
         check(self._lib.arbo_mcmc_propose(self._h, int(it), _dp(out), None))
@@ -177,6 +181,30 @@ def sim_seed(base: int, chain: int, replicate: int, it: int) -> int:
     return (x * 0xBF58476D1CE4E5B9) & (2**64 - 1)
 
 
+class StepAdapter:
+    """Burn-in adaptation of the random-walk scale: every `every` iterations up to `until`, all
+    standard deviations are multiplied by exp(2 * (acceptance - target)) (acceptance of the last
+    block over all chains), clipped to [1/2, 2] per block. Iterations after `until` use fixed steps,
+    so the recorded chain from there on is a valid Metropolis-Hastings chain; the adaptation reads
+    only device counters, so plain, batched and delayed drivers adapt alike."""
+
+    def __init__(self, until: int = 0, every: int = 10, target: float = 0.234):
+        self.until, self.every, self.target = int(until), int(every), float(target)
+        self.last = None
+        self.history = []
+
+    def __call__(self, m: "MCMC", it: int) -> None:
+        if it > self.until or it % self.every:
+            return
+        acc = int(m.state()["accepted"].sum())
+        if self.last is not None:
+            rate = (acc - self.last) / float(m.C * self.every)
+            f = float(np.clip(np.exp(2.0 * (rate - self.target)), 0.5, 2.0))
+            m.set_step(m.step_sd * f)
+            self.history.append((it, rate, f))
+        self.last = acc
+
+
 def _simulate_alone(sim: Simulation):
     sim.init()
     sim.run()
@@ -202,7 +230,7 @@ def start(m: MCMC, theta0: np.ndarray, sims: List[Simulation], batch: Optional[B
 
 
 def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
-              on_iter: Optional[Callable] = None) -> dict:
+              on_iter: Optional[Callable] = None, adapt: Optional[StepAdapter] = None) -> dict:
     """One proposal at a time: for every chain in turn, its proposal is simulated by the same
     handle(s) (replicates of one handle each) and accepted or rejected."""
     sims = sims if sims is not None else m.make_sims(m.R)
@@ -219,13 +247,16 @@ def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simul
             sim_s += time.perf_counter() - t1
             m.calc_log_likelihood(sims[:m.R], c, c + 1)
             m.next_step(it, c, c + 1)
+        if adapt:
+            adapt(m, it)
         if on_iter:
             on_iter(it)
     return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * iters}
 
 
 def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
-                batch: Optional[Batch] = None, on_iter: Optional[Callable] = None) -> dict:
+                batch: Optional[Batch] = None, on_iter: Optional[Callable] = None,
+                adapt: Optional[StepAdapter] = None) -> dict:
     """All chains together: the proposals of the C chains (times replicates) are simulated by one
     batch, then the likelihoods and the acceptance steps of all chains run as one kernel each."""
     sims = sims if sims is not None else m.make_sims(m.C * m.R)
@@ -245,6 +276,8 @@ def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Sim
         sim_s += time.perf_counter() - t1
         m.calc_log_likelihood(sims, 0, m.C)
         m.next_step(it)
+        if adapt:
+            adapt(m, it)
         if on_iter:
             on_iter(it)
     if own:
@@ -253,7 +286,8 @@ def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Sim
 
 
 def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np.ndarray], np.ndarray],
-                sims: Optional[List[Simulation]] = None, on_iter: Optional[Callable] = None) -> dict:
+                sims: Optional[List[Simulation]] = None, on_iter: Optional[Callable] = None,
+                adapt: Optional[StepAdapter] = None) -> dict:
     """Delayed-acceptance Metropolis-Hastings (Christen & Fox 2005). ``surrogate(theta[C, D])``
     returns an approximate log-likelihood per chain. Stage 1 screens every proposal with it (GPU,
     FP64); only the proposals that pass are simulated, together in one batch of as many handles as
@@ -290,6 +324,8 @@ def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np
                 for j, c in enumerate(passed):
                     m.calc_log_likelihood(sims[j * m.R:(j + 1) * m.R], int(c), int(c) + 1)
             m.next_step(it, screened=True)
+            if adapt:
+                adapt(m, it)
             if on_iter:
                 on_iter(it)
     finally:

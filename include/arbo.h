@@ -437,6 +437,8 @@ int arbo_mcmc_destroy(arbo_mcmc* m);
 /* Current state of every chain (chains * params doubles); also loaded as the proposals so that
  * arbo_mcmc_loglik(..., current = 1) can evaluate it, and recorded as iteration 0. */
 int arbo_mcmc_set_state(arbo_mcmc* m, const double* theta, void* stream);
+/* Replaces the random-walk standard deviations (params doubles), e.g. while adapting during burn-in. */
+int arbo_mcmc_set_step(arbo_mcmc* m, const double* step);
 /* MCMC::propose (cpp/MCMC.cpp:100-137) without the adaptive covariance: theta + step * N(0, 1)
  * per parameter. out (optional, chains * params) receives the proposals. */
 int arbo_mcmc_propose(arbo_mcmc* m, uint32_t iter, double* out, void* stream);
