@@ -149,3 +149,38 @@ def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt
     mb, md = np.array(b["mean"]), np.array(d["mean"])
     out["delayed_mean_rel_diff_vs_exact"] = (np.abs(md - mb) / np.abs(mb)).tolist()
     return out
+
+
+def main(argv=None):
+    """python -m arbo_gpu_fit_gb300.fit --population small --iters 300 --adapt 100 --plain-iters 20
+    --train-runs 4096 --epochs 60 [--out result.json]"""
+    import argparse
+    import json
+
+    from . import _native
+
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--population", choices=["small", "large"], default="small")
+    ap.add_argument("--chains", type=int, default=64)
+    ap.add_argument("--iters", type=int, default=300)
+    ap.add_argument("--adapt", type=int, default=100)
+    ap.add_argument("--plain-iters", type=int, default=20)
+    ap.add_argument("--train-runs", type=int, default=4096)
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+    _native.check(_native.load().arbo_set_device(a.device))
+    t0 = time.perf_counter()
+    r = compare(a.population, chains=a.chains, iters=a.iters, adapt_until=a.adapt, plain_iters=a.plain_iters,
+                train_runs=a.train_runs, epochs=a.epochs)
+    r["total_s"] = time.perf_counter() - t0
+    text = json.dumps(r, indent=1)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text)
+    print(text)
+
+
+if __name__ == "__main__":
+    main()
