@@ -207,7 +207,7 @@ int arbo_arch_param_query(arbo_arch_param* a, int device)
     a->demogBlock = 256;
     a->demogUnroll = 2;
     a->foiBlock = 256;
-    a->infectBlock = 256;
+    a->infectBlock = 128;  // two communities per CTA: fastest on the large workload (launch-shape sweep)
     a->graphSteps = 64;
     a->demogPipeline = 0;
     int n = 0;

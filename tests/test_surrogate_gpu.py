@@ -64,3 +64,20 @@ def test_training_lowers_loss(gpu):
             net.train_step(x[i:i + 256], t[i:i + 256], 2e-3)
     last = net.gradients(x[:256], t[:256])
     assert last < 0.1 * first, (first, last)
+
+
+def test_surrogate_pipeline_on_simulator_runs(gpu):
+    # Training data from batched simulator runs, a small network fitted to it, and the
+    # surrogate likelihood of observed data: the path delayed acceptance uses.
+    from arbo_gpu_fit_gb300 import configs, mcmc
+    from arbo_gpu_fit_gb300.surrogate import Surrogate, training_set
+
+    w = configs.scaled(800, 2400, 3, 120, seed=4, sigma=0.3, bitingRate=0.9, nInitialInf=30.0, mInitialInf=90.0)
+    theta, inc = training_set(w, 48, 4, seed=1, batch_size=16)
+    assert theta.shape == (48, 6) and inc.shape == (48, 4, 4) and inc.sum() > 0
+    sur = Surrogate(4, 4, hidden=64, hidden_layers=2, seed=2, max_batch=64)
+    losses = sur.fit(theta, inc, epochs=80, batch=16, lr=3e-3)
+    assert losses[-1] < 0.5 * losses[0]
+    obs = mcmc.synthetic_data(w, theta[0], months=4, seed=2)
+    ll = sur.loglik(theta[:5], obs)
+    assert ll.shape == (5,) and np.all(np.isfinite(ll))
