@@ -9,6 +9,8 @@
 //   forward  Z_l  = H_{l-1} W_l^T          A = H_{l-1} [B][in],  B = W_l  [out][in]
 //   backward dH   = dZ_l W_l               A = dZ_l    [B][out], B = W_l^T [in][out]
 //   weights  dW_l = dZ_l^T H_{l-1}         A = dZ_l^T  [out][B], B = H_{l-1}^T [in][B]
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -46,11 +48,11 @@ struct GemmArgs {
     uint32_t* err;       // bit 0: an mbarrier wait ran out
 };
 
-constexpr uint32_t kTileM = 128, kTileN = 128, kTileK = 64;
-constexpr uint32_t kOperandBytes = kTileM * kTileK * 2;  // one operand chunk (16 KB)
-// Dynamic shared memory per CTA: the two operand chunks, padded so that at most four CTAs share an
-// SM and their 128-column accumulators fit the 512 tensor-memory columns without waiting.
-constexpr uint32_t kGemmSmem = 56 * 1024;
+constexpr uint32_t kTileM = 128, kTileK = 64, kStages = 4;
+constexpr uint32_t kMaxTileN = 256;
+// Dynamic shared memory: kStages stages of A (128 x 64) and B (up to 256 x 64) BF16 chunks plus
+// 1 KB of alignment slack.
+constexpr uint32_t kGemmSmem = kStages * (kTileM + kMaxTileN) * kTileK * 2 + 1024;
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
 __device__ __forceinline__ float dsilu(float z)
@@ -59,59 +61,86 @@ __device__ __forceinline__ float dsilu(float z)
     return s * (1.0f + z * (1.0f - s));
 }
 
-// One 128 x 128 output tile per CTA of 128 threads. The K loop stages 64-wide chunks of both
-// operands in the core-matrix layout, one thread issues four K=16 tensor-core products per chunk
-// and commits them to an mbarrier; every thread waits (bounded) before the chunk is overwritten.
-// The epilogue reads the accumulator from tensor memory, one row per thread.
-__global__ void __launch_bounds__(128, 1) k_gemm_tn(GemmArgs g)
+// One kTileM x tn output tile per CTA of 128 threads (tn = 128 or 256, a launch parameter).
+// Operands arrive by TMA: each 64-wide K chunk of A and B is eight 2-D boxes of {8 elements x
+// rows}, every box landing as one K column of 8-row x 16-byte core matrices (K-adjacent core
+// matrices 2048 bytes apart for A, tn*16 for B; 8-row groups 128 bytes apart). kStages chunks are
+// in flight: thread 0 waits for a stage's "full" barrier, issues its four K=16 tcgen05 products,
+// commits them to the stage's "empty" barrier, and refills the stage used one chunk earlier once
+// its products are done, so the tensor core always has a chunk queued while the next loads run.
+// Every wait is bounded; on a timeout the CTA records the error, drains what it issued (bounded)
+// and frees its tensor memory. The epilogue reads the FP32 accumulator with tcgen05.ld, one row
+// per thread.
+__global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUtensorMap mapA,
+                                                   const __grid_constant__ CUtensorMap mapB, GemmArgs g, uint32_t tn)
 {
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ unsigned long long bar;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ unsigned long long full[kStages], empty[kStages], done;
     __shared__ uint32_t tmem_slot;
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const uint32_t m0 = blockIdx.x * kTileM, n0 = blockIdx.y * kTileN;
-    const uint32_t nt = min(kTileN, g.N - n0);
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + kOperandBytes;
-    if (warp == 0) tc_alloc(&tmem_slot, kTileN);
-    if (tid == 0) tc_bar_init(&bar, 1);
+    const uint32_t m0 = blockIdx.x * kTileM, n0 = blockIdx.y * tn;
+    const uint32_t nt = min(tn, g.N - n0);
+    const uint32_t aBytes = kTileM * kTileK * 2, bBytes = tn * kTileK * 2, stageBytes = aBytes + bBytes;
+    if (warp == 0) tc_alloc(&tmem_slot, tn);
+    if (tid == 0) {
+        for (uint32_t s = 0; s < kStages; ++s) {
+            tc_bar_init(&full[s], 1);
+            tc_bar_init(&empty[s], 1);
+        }
+        tc_bar_init(&done, 1);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t idesc = tc_idesc_bf16(kTileM, nt);
-    uint32_t phase = 0;
+    const uint32_t nk = (g.K + kTileK - 1) / kTileK;
     bool ok = true;
-    for (uint32_t k0 = 0; k0 < g.K && ok; k0 += kTileK) {
-        for (uint32_t p = tid; p < kTileM * 8; p += blockDim.x) {
-            const uint32_t r = p >> 3, kb = p & 7u, k = k0 + kb * 8;
-            const uint32_t off = (r >> 3) * 1024 + kb * 128 + (r & 7u) * 16;
-            uint4 va = make_uint4(0, 0, 0, 0), vb = va;
-            if (m0 + r < g.M && k < g.K) va = *reinterpret_cast<const uint4*>(g.A + (size_t)(m0 + r) * g.lda + k);
-            if (n0 + r < g.N && k < g.K) vb = *reinterpret_cast<const uint4*>(g.B + (size_t)(n0 + r) * g.ldb + k);
-            *reinterpret_cast<uint4*>(sA + off) = va;
-            *reinterpret_cast<uint4*>(sB + off) = vb;
-        }
-        tc_fence_smem();
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t ks = min(4u, (g.K - k0) / 16);
-            for (uint32_t kk = 0; kk < ks; ++kk) {
-                const uint64_t ad = tc_desc(tc_smem(sA) + kk * 256, 128, 1024);
-                const uint64_t bd = tc_desc(tc_smem(sB) + kk * 256, 128, 1024);
-                tc_mma(tmem, ad, bd, idesc, k0 > 0 || kk > 0);
+    if (tid == 0) {
+        const uint32_t idesc = tc_idesc_bf16(kTileM, nt);
+        auto load = [&](uint32_t c) {
+            const uint32_t s = c % kStages;
+            uint8_t* sa = smem + s * stageBytes;
+            uint8_t* sb = sa + aBytes;
+            tc_bar_expect_tx(&full[s], stageBytes);
+            for (uint32_t kb = 0; kb < 8; ++kb) {
+                const int32_t x = (int32_t)(c * kTileK + kb * 8);
+                tc_tma_load_2d(sa + kb * kTileM * 16, &mapA, x, (int32_t)m0, &full[s]);
+                tc_tma_load_2d(sb + kb * tn * 16, &mapB, x, (int32_t)n0, &full[s]);
             }
-            tc_commit(&bar);
+        };
+        for (uint32_t c = 0; c < nk && c < kStages; ++c) load(c);
+        for (uint32_t c = 0; c < nk && ok; ++c) {
+            const uint32_t s = c % kStages;
+            ok = tc_bar_wait(&full[s], (c / kStages) & 1u);
+            if (!ok) break;
+            tc_fence_after();
+            const uint32_t sa = tc_smem(smem + s * stageBytes), sb = sa + aBytes;
+            const uint32_t ks = min(4u, (g.K - c * kTileK + 15) / 16);
+            for (uint32_t kk = 0; kk < ks; ++kk) {
+                const uint64_t ad = tc_desc(sa + kk * 2 * kTileM * 16, kTileM * 16, 128);
+                const uint64_t bd = tc_desc(sb + kk * 2 * tn * 16, tn * 16, 128);
+                tc_mma(tmem, ad, bd, idesc, c > 0 || kk > 0);
+            }
+            tc_commit(&empty[s]);
+            // Refill the stage of the previous chunk once its products have finished.
+            if (c >= 1 && c - 1 + kStages < nk) {
+                const uint32_t p = c - 1, sp = p % kStages;
+                ok = tc_bar_wait(&empty[sp], (p / kStages) & 1u);
+                if (ok) load(p + kStages);
+            }
         }
-        ok = tc_bar_wait(&bar, phase);
-        phase ^= 1u;
-        ok = __syncthreads_and(ok);
+        tc_commit(&done);  // arrives when every product issued above has completed
     }
+    ok = tc_bar_wait(&done, 0) && ok;
+    ok = __syncthreads_and(ok);
     tc_fence_after();
     if (!ok) {
-        if (tid == 0) atomicOr(g.err, 1u);
-        tc_bar_wait(&bar, phase ^ 1u);  // bounded: whatever is still in flight
+        if (tid == 0) {
+            atomicOr(g.err, 1u);
+            // Drain: every stage's last load and products (bounded waits).
+            for (uint32_t s = 0; s < kStages; ++s) tc_bar_wait(&empty[s], 0), tc_bar_wait(&full[s], 0);
+        }
     } else {
         const uint32_t row = m0 + warp * 32 + lane;
         const bool live = row < g.M;
@@ -143,7 +172,50 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(GemmArgs g)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_dealloc(tmem, kTileN);
+    if (warp == 0) tc_dealloc(tmem, tn);
+}
+
+// Tensor map of a row-major BF16 matrix [rows][ld] whose first `cols` columns are the operand:
+// boxes of {8 columns x box_rows rows}, zero fill outside.
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int tensor_map(CUtensorMap* map, const bf16* base, uint32_t rows, uint32_t cols, uint32_t ld, uint32_t box_rows)
+{
+    if (!g_encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return set_error(ARBO_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+        g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    if ((reinterpret_cast<uintptr_t>(base) & 15u) || (ld * 2) % 16)
+        return set_error(ARBO_ERR_INVALID, "tensor map: base and row pitch must be 16-byte aligned");
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {8, box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(ARBO_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return ARBO_OK;
+}
+
+// Launches C = A B^T with the epilogue of g: 128 x 256 tiles when that still gives at least one
+// tile per SM, else 128 x 128. Returns a cudaError_t (invalid value when a tensor map cannot be
+// built; the reason is then in arbo_last_error).
+int gemm_launch(const GemmArgs& g, cudaStream_t st, uint32_t num_sm)
+{
+    const uint32_t mt = (g.M + kTileM - 1) / kTileM;
+    const uint32_t tn = (g.N >= 256 && mt * ((g.N + 255) / 256) >= num_sm) ? 256u : 128u;
+    CUtensorMap ma, mb;
+    if (tensor_map(&ma, g.A, g.M, g.K, g.lda, kTileM) || tensor_map(&mb, g.B, g.N, g.K, g.ldb, tn))
+        return (int)cudaErrorInvalidValue;
+    const dim3 grid(mt, (g.N + tn - 1) / tn);
+    k_gemm_tn<<<grid, 128, kGemmSmem, st>>>(ma, mb, g, tn);
+    return (int)cudaGetLastError();
 }
 
 // Inputs: FP32 [n][nin] -> BF16 [n][ldx] (zero padded) and transposed [ldx][ldt].
@@ -249,6 +321,7 @@ struct arbo_mlp {
     float *xin = nullptr, *tin = nullptr, *loss = nullptr;
     uint32_t* err = nullptr;
     uint32_t steps = 0;
+    uint32_t num_sm = 152;
     std::vector<void*> allocs;
 };
 
@@ -259,9 +332,7 @@ int mlp_gemm(arbo_mlp* n, const bf16* A, uint32_t lda, const bf16* B, uint32_t l
              bf16* outb, uint32_t ldob, bf16* outt, uint32_t ldot, cudaStream_t st)
 {
     GemmArgs g{A, B, lda, ldb, M, N, K, epi, bias, zprev, ldz, outf, ldof, outb, ldob, outt, ldot, n->err};
-    const dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
-    k_gemm_tn<<<grid, 128, kGemmSmem, st>>>(g);
-    return (int)cudaGetLastError();
+    return gemm_launch(g, st, n->num_sm);
 }
 
 int mlp_forward(arbo_mlp* n, uint32_t rows, cudaStream_t st)
@@ -341,11 +412,10 @@ int arbo_mlp_create(uint32_t n_in, uint32_t hidden, uint32_t hidden_layers, uint
     *out = nullptr;
     arbo_mlp* n = new arbo_mlp();
     UCUDA(cudaGetDevice(&n->device));
-    static bool attr = false;
-    if (!attr) {
-        UCUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
-        attr = true;
-    }
+    UCUDA(cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, n->device) == cudaSuccess && sms > 0)
+        n->num_sm = (uint32_t)sms;
     n->L = hidden_layers + 1;
     n->nin = n_in;
     n->nout = n_out;
@@ -554,13 +624,16 @@ int arbo_tc_gemm(const float* a, const float* b, uint32_t M, uint32_t N, uint32_
     cudaMemcpy(db, hb.data(), hb.size() * 2, cudaMemcpyHostToDevice);
     cudaMemset(derr, 0, 4);
     GemmArgs g{da, db, K, K, M, N, K, kEpiStore, nullptr, nullptr, 0, dc, N, nullptr, 0, nullptr, 0, derr};
-    const dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
+    int sms = 152, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    k_gemm_tn<<<grid, 128, kGemmSmem>>>(g);
+    int le = gemm_launch(g, nullptr, (uint32_t)sms);
+    const std::string map_err = le ? std::string(arbo_last_error()) : std::string();
     cudaEventRecord(e0);
-    for (uint32_t r = 0; r < reps; ++r) k_gemm_tn<<<grid, 128, kGemmSmem>>>(g);
+    for (uint32_t r = 0; r < reps && !le; ++r) le = gemm_launch(g, nullptr, (uint32_t)sms);
     cudaEventRecord(e1);
     cudaError_t ce = cudaEventSynchronize(e1);
     float t = 0;
@@ -572,6 +645,7 @@ int arbo_tc_gemm(const float* a, const float* b, uint32_t M, uint32_t N, uint32_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cleanup();
+    if (le) return ufail(ARBO_ERR_CUDA, "arbo_tc_gemm: launch failed: " + map_err + " " + cudaGetErrorString((cudaError_t)le));
     if (ce != cudaSuccess) return ufail(ARBO_ERR_CUDA, std::string("arbo_tc_gemm: ") + cudaGetErrorString(ce));
     if (herr) return ufail(ARBO_ERR_CUDA, "arbo_tc_gemm: an mbarrier wait ran out");
     return ARBO_OK;

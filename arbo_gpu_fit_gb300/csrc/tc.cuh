@@ -8,6 +8,7 @@
 // i.e. core matrices adjacent along K are 128 bytes apart (the descriptor's leading-dimension
 // offset) and groups of 8 rows are SBO apart (its stride offset).
 #pragma once
+#include <cuda.h>
 #include <stdint.h>
 
 namespace arbo {
@@ -99,6 +100,24 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// One arrival on `bar` that also announces `bytes` of asynchronous transfers for its current phase.
+__device__ __forceinline__ void tc_bar_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem(bar)), "r"(bytes) : "memory");
+}
+
+// Tiled TMA load of a 2-D box at element coordinates (x innermost, y) into shared memory,
+// completing on `bar`. x times the element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tc_tma_load_2d(void* dst, const CUtensorMap* map, int32_t x, int32_t y,
+                                               unsigned long long* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            tc_smem(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc_smem(bar))
+        : "memory");
 }
 
 }  // namespace arbo
