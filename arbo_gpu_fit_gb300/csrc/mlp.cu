@@ -62,15 +62,14 @@ __device__ __forceinline__ float dsilu(float z)
 }
 
 // One kTileM x tn output tile per CTA of 128 threads (tn = 128 or 256, a launch parameter).
-// Operands arrive by TMA: each 64-wide K chunk of A and B is eight 2-D boxes of {8 elements x
-// rows}, every box landing as one K column of 8-row x 16-byte core matrices (K-adjacent core
-// matrices 2048 bytes apart for A, tn*16 for B; 8-row groups 128 bytes apart). kStages chunks are
-// in flight: thread 0 waits for a stage's "full" barrier, issues its four K=16 tcgen05 products,
-// commits them to the stage's "empty" barrier, and refills the stage used one chunk earlier once
-// its products are done, so the tensor core always has a chunk queued while the next loads run.
-// Every wait is bounded; on a timeout the CTA records the error, drains what it issued (bounded)
-// and frees its tensor memory. The epilogue reads the FP32 accumulator with tcgen05.ld, one row
-// per thread.
+// Operands arrive by TMA in the 128-byte-swizzled K-major layout: one box of {64 elements x rows}
+// per operand and 64-wide K chunk (A: 16 KB, B: tn x 128 bytes). kStages chunks are in flight:
+// thread 0 waits for a stage's "full" barrier, issues its four K=16 tcgen05 products (descriptor
+// start advanced 32 bytes per slice), commits them to the stage's "empty" barrier, and refills the
+// stage used one chunk earlier once its products are done, so the tensor core always has a chunk
+// queued while the next loads run. Every wait is bounded; on a timeout the CTA records the error,
+// drains what it issued (bounded) and frees its tensor memory. The epilogue reads the FP32
+// accumulator with tcgen05.ld, one row per thread.
 __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUtensorMap mapA,
                                                    const __grid_constant__ CUtensorMap mapB, GemmArgs g, uint32_t tn)
 {
@@ -103,11 +102,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
             uint8_t* sa = smem + s * stageBytes;
             uint8_t* sb = sa + aBytes;
             tc_bar_expect_tx(&full[s], stageBytes);
-            for (uint32_t kb = 0; kb < 8; ++kb) {
-                const int32_t x = (int32_t)(c * kTileK + kb * 8);
-                tc_tma_load_2d(sa + kb * kTileM * 16, &mapA, x, (int32_t)m0, &full[s]);
-                tc_tma_load_2d(sb + kb * tn * 16, &mapB, x, (int32_t)n0, &full[s]);
-            }
+            tc_tma_load_2d(sa, &mapA, (int32_t)(c * kTileK), (int32_t)m0, &full[s]);
+            tc_tma_load_2d(sb, &mapB, (int32_t)(c * kTileK), (int32_t)n0, &full[s]);
         };
         for (uint32_t c = 0; c < nk && c < kStages; ++c) load(c);
         for (uint32_t c = 0; c < nk && ok; ++c) {
@@ -118,8 +114,8 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
             const uint32_t sa = tc_smem(smem + s * stageBytes), sb = sa + aBytes;
             const uint32_t ks = min(4u, (g.K - c * kTileK + 15) / 16);
             for (uint32_t kk = 0; kk < ks; ++kk) {
-                const uint64_t ad = tc_desc(sa + kk * 2 * kTileM * 16, kTileM * 16, 128);
-                const uint64_t bd = tc_desc(sb + kk * 2 * tn * 16, tn * 16, 128);
+                const uint64_t ad = tc_desc_sw128(sa + kk * 32);
+                const uint64_t bd = tc_desc_sw128(sb + kk * 32);
                 tc_mma(tmem, ad, bd, idesc, c > 0 || kk > 0);
             }
             tc_commit(&empty[s]);
@@ -176,7 +172,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUte
 }
 
 // Tensor map of a row-major BF16 matrix [rows][ld] whose first `cols` columns are the operand:
-// boxes of {8 columns x box_rows rows}, zero fill outside.
+// boxes of {64 columns x box_rows rows} written 128-byte swizzled, zero fill outside.
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 int tensor_map(CUtensorMap* map, const bf16* base, uint32_t rows, uint32_t cols, uint32_t ld, uint32_t box_rows)
@@ -194,10 +190,10 @@ int tensor_map(CUtensorMap* map, const bf16* base, uint32_t rows, uint32_t cols,
         return set_error(ARBO_ERR_INVALID, "tensor map: base and row pitch must be 16-byte aligned");
     const cuuint64_t dims[2] = {cols, rows};
     const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {8, box_rows};
+    const cuuint32_t box[2] = {64, box_rows};
     const cuuint32_t es[2] = {1, 1};
     const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(ARBO_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
     return ARBO_OK;

@@ -25,6 +25,16 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+// Descriptor of a K-major operand in the 128-byte-swizzled layout that a TMA copy with
+// CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 128 bytes (64 BF16 along K), the 16-byte chunks of
+// row r permuted by r mod 8, 8-row groups 1024 bytes apart (stride offset). The start address
+// advances by 32 bytes per K=16 slice inside the row; the leading offset is unused (encoded 1).
+__device__ __forceinline__ uint64_t tc_desc_sw128(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N.
 __host__ __device__ constexpr uint32_t tc_idesc_bf16(uint32_t M, uint32_t N)
 {
