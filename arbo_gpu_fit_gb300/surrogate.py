@@ -193,3 +193,27 @@ def training_set(workload: configs.Workload, n: int, months: int, seed: int = 0,
         for s in sims:
             s.close()
     return theta, inc
+
+
+def main(argv=None):
+    """python -m arbo_gpu_fit_gb300.surrogate gemm M N K [reps]: one tensor-core product of
+    standard-normal inputs (rounded to BF16), timed over reps launches; prints M N K ms TFLOP/s."""
+    import sys
+
+    from . import _native
+
+    args = list(sys.argv[1:] if argv is None else argv)
+    if len(args) < 4 or args[0] != "gemm":
+        raise SystemExit(main.__doc__)
+    M, N, K = (int(x) for x in args[1:4])
+    reps = int(args[4]) if len(args) > 4 else 20
+    _native.check(_native.load().arbo_set_device(0))
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal((M, K)).astype(np.float32)
+    b = rng.standard_normal((N, K)).astype(np.float32)
+    _, ms = tc_gemm(a, b, reps=reps)
+    print(M, N, K, ms, 2.0 * M * N * K / (ms * 1e-3) / 1e12 if ms else 0.0)
+
+
+if __name__ == "__main__":
+    main()
