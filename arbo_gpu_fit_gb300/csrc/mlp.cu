@@ -61,114 +61,126 @@ __device__ __forceinline__ float dsilu(float z)
     return s * (1.0f + z * (1.0f - s));
 }
 
-// One kTileM x tn output tile per CTA of 128 threads (tn = 128 or 256, a launch parameter).
-// Operands arrive by TMA in the 128-byte-swizzled K-major layout: one box of {64 elements x rows}
-// per operand and 64-wide K chunk (A: 16 KB, B: tn x 128 bytes). kStages chunks are in flight:
-// thread 0 waits for a stage's "full" barrier, issues its four K=16 tcgen05 products (descriptor
-// start advanced 32 bytes per slice), commits them to the stage's "empty" barrier, and refills the
-// stage used one chunk earlier once its products are done, so the tensor core always has a chunk
-// queued while the next loads run. Every wait is bounded; on a timeout the CTA records the error,
-// drains what it issued (bounded) and frees its tensor memory. The epilogue reads the FP32
-// accumulator with tcgen05.ld, one row per thread.
-__global__ void __launch_bounds__(128, 1) k_gemm_tn(const __grid_constant__ CUtensorMap mapA,
+// Persistent, warp-specialised product: each CTA (192 threads) walks output tiles of kTileM x tn
+// (tn = 128 or 256) in a grid-stride loop.
+//   warp 0, one thread: TMA producer. Each 64-wide K chunk of A and B is one box per operand in
+//     the 128-byte-swizzled K-major layout; kStages chunks are in flight ("full" / "empty"
+//     mbarriers per stage).
+//   warp 1, one thread: issues the four K=16 tcgen05 products of each chunk into one of two
+//     tensor-memory accumulators (tile parity), commits each chunk to the stage's "empty" barrier
+//     and each finished tile to the accumulator's "full" barrier.
+//   warps 2-5: epilogue. Warp w reads tensor-memory lanes 32*(w mod 4) .. +31 with tcgen05.ld,
+//     applies the fused epilogue, then releases the accumulator ("empty", four arrivals), so the
+//     products of the next tile overlap the epilogue of this one.
+// Every wait is bounded; a role that runs out records the error and stops, which bounds the waits
+// of the others; tensor memory is freed at the end in every case.
+__global__ void __launch_bounds__(192, 1) k_gemm_tn(const __grid_constant__ CUtensorMap mapA,
                                                    const __grid_constant__ CUtensorMap mapB, GemmArgs g, uint32_t tn)
 {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ unsigned long long full[kStages], empty[kStages], done;
+    __shared__ unsigned long long full[kStages], empty[kStages], acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_slot;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const uint32_t m0 = blockIdx.x * kTileM, n0 = blockIdx.y * tn;
-    const uint32_t nt = min(tn, g.N - n0);
     const uint32_t aBytes = kTileM * kTileK * 2, bBytes = tn * kTileK * 2, stageBytes = aBytes + bBytes;
-    if (warp == 0) tc_alloc(&tmem_slot, tn);
+    const uint32_t mtiles = (g.M + kTileM - 1) / kTileM, ntiles = (g.N + tn - 1) / tn, tiles = mtiles * ntiles;
+    const uint32_t nk = (g.K + kTileK - 1) / kTileK;
+    if (warp == 0) tc_alloc(&tmem_slot, 2 * tn);
     if (tid == 0) {
         for (uint32_t s = 0; s < kStages; ++s) {
             tc_bar_init(&full[s], 1);
             tc_bar_init(&empty[s], 1);
         }
-        tc_bar_init(&done, 1);
+        for (uint32_t a = 0; a < 2; ++a) {
+            tc_bar_init(&acc_full[a], 1);
+            tc_bar_init(&acc_empty[a], 4);
+        }
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t nk = (g.K + kTileK - 1) / kTileK;
     bool ok = true;
-    if (tid == 0) {
-        const uint32_t idesc = tc_idesc_bf16(kTileM, nt);
-        auto load = [&](uint32_t c) {
-            const uint32_t s = c % kStages;
-            uint8_t* sa = smem + s * stageBytes;
-            uint8_t* sb = sa + aBytes;
-            tc_bar_expect_tx(&full[s], stageBytes);
-            tc_tma_load_2d(sa, &mapA, (int32_t)(c * kTileK), (int32_t)m0, &full[s]);
-            tc_tma_load_2d(sb, &mapB, (int32_t)(c * kTileK), (int32_t)n0, &full[s]);
-        };
-        for (uint32_t c = 0; c < nk && c < kStages; ++c) load(c);
-        for (uint32_t c = 0; c < nk && ok; ++c) {
-            const uint32_t s = c % kStages;
-            ok = tc_bar_wait(&full[s], (c / kStages) & 1u);
+    if (warp == 0 && lane == 0) {  // producer
+        uint32_t kc = 0;
+        for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+            const uint32_t m0 = (t % mtiles) * kTileM, n0 = (t / mtiles) * tn;
+            for (uint32_t c = 0; c < nk && ok; ++c, ++kc) {
+                const uint32_t s = kc % kStages;
+                if (kc >= kStages) ok = tc_bar_wait(&empty[s], ((kc / kStages) - 1) & 1u);
+                if (!ok) break;
+                uint8_t* sa = smem + s * stageBytes;
+                tc_bar_expect_tx(&full[s], stageBytes);
+                tc_tma_load_2d(sa, &mapA, (int32_t)(c * kTileK), (int32_t)m0, &full[s]);
+                tc_tma_load_2d(sa + aBytes, &mapB, (int32_t)(c * kTileK), (int32_t)n0, &full[s]);
+            }
+        }
+    } else if (warp == 1 && lane == 0) {  // tensor-core issuer
+        uint32_t kc = 0, li = 0;
+        for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++li) {
+            const uint32_t n0 = (t / mtiles) * tn, nt = min(tn, g.N - n0), a = li & 1u;
+            if (li >= 2) ok = tc_bar_wait(&acc_empty[a], ((li >> 1) - 1) & 1u);
             if (!ok) break;
             tc_fence_after();
-            const uint32_t sa = tc_smem(smem + s * stageBytes), sb = sa + aBytes;
-            const uint32_t ks = min(4u, (g.K - c * kTileK + 15) / 16);
-            for (uint32_t kk = 0; kk < ks; ++kk) {
-                const uint64_t ad = tc_desc_sw128(sa + kk * 32);
-                const uint64_t bd = tc_desc_sw128(sb + kk * 32);
-                tc_mma(tmem, ad, bd, idesc, c > 0 || kk > 0);
+            const uint32_t idesc = tc_idesc_bf16(kTileM, nt), d = tmem + a * tn;
+            for (uint32_t c = 0; c < nk; ++c, ++kc) {
+                const uint32_t s = kc % kStages;
+                ok = tc_bar_wait(&full[s], (kc / kStages) & 1u);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t sa = tc_smem(smem + s * stageBytes), sb = sa + aBytes;
+                const uint32_t ks = min(4u, (g.K - c * kTileK + 15) / 16);
+                for (uint32_t kk = 0; kk < ks; ++kk)
+                    tc_mma(d, tc_desc_sw128(sa + kk * 32), tc_desc_sw128(sb + kk * 32), idesc, c > 0 || kk > 0);
+                tc_commit(&empty[s]);
             }
-            tc_commit(&empty[s]);
-            // Refill the stage of the previous chunk once its products have finished.
-            if (c >= 1 && c - 1 + kStages < nk) {
-                const uint32_t p = c - 1, sp = p % kStages;
-                ok = tc_bar_wait(&empty[sp], (p / kStages) & 1u);
-                if (ok) load(p + kStages);
-            }
+            tc_commit(&acc_full[a]);
         }
-        tc_commit(&done);  // arrives when every product issued above has completed
-    }
-    ok = tc_bar_wait(&done, 0) && ok;
-    ok = __syncthreads_and(ok);
-    tc_fence_after();
-    if (!ok) {
-        if (tid == 0) {
-            atomicOr(g.err, 1u);
-            // Drain: every stage's last load and products (bounded waits).
-            for (uint32_t s = 0; s < kStages; ++s) tc_bar_wait(&empty[s], 0), tc_bar_wait(&full[s], 0);
-        }
-    } else {
-        const uint32_t row = m0 + warp * 32 + lane;
-        const bool live = row < g.M;
-        for (uint32_t c0 = 0; c0 < nt; c0 += 16) {
-            float v[16];
-            tc_ld16(tmem + ((warp * 32u) << 16) + c0, v);
-            if (!live) continue;
+    } else if (warp >= 2) {  // epilogue
+        const uint32_t quarter = warp & 3u;
+        uint32_t li = 0;
+        for (uint32_t t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++li) {
+            const uint32_t m0 = (t % mtiles) * kTileM, n0 = (t / mtiles) * tn, nt = min(tn, g.N - n0), a = li & 1u;
+            ok = __all_sync(0xffffffffu, tc_bar_wait(&acc_full[a], (li >> 1) & 1u));  // warp-uniform
+            if (!ok) break;
+            tc_fence_after();
+            const uint32_t row = m0 + quarter * 32 + lane;
+            const bool live = row < g.M;
+            for (uint32_t c0 = 0; c0 < nt; c0 += 16) {
+                float v[16];
+                tc_ld16(tmem + a * tn + ((quarter * 32u) << 16) + c0, v);
+                if (!live) continue;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const uint32_t n = n0 + c0 + j;
-                float x = v[j];
-                if (g.epi == kEpiHidden) {
-                    x += g.bias[n];
-                    g.outf[(size_t)row * g.ldof + n] = x;
-                    const bf16 h = __float2bfloat16_rn(silu(x));
-                    g.outb[(size_t)row * g.ldob + n] = h;
-                    g.outt[(size_t)n * g.ldot + row] = h;
-                } else if (g.epi == kEpiLinear) {
-                    g.outf[(size_t)row * g.ldof + n] = x + g.bias[n];
-                } else if (g.epi == kEpiBackward) {
-                    const bf16 dz = __float2bfloat16_rn(x * dsilu(g.zprev[(size_t)row * g.ldz + n]));
-                    g.outb[(size_t)row * g.ldob + n] = dz;
-                    g.outt[(size_t)n * g.ldot + row] = dz;
-                } else {
-                    g.outf[(size_t)row * g.ldof + n] = x;
+                for (int j = 0; j < 16; ++j) {
+                    const uint32_t n = n0 + c0 + j;
+                    float x = v[j];
+                    if (g.epi == kEpiHidden) {
+                        x += g.bias[n];
+                        g.outf[(size_t)row * g.ldof + n] = x;
+                        const bf16 h = __float2bfloat16_rn(silu(x));
+                        g.outb[(size_t)row * g.ldob + n] = h;
+                        g.outt[(size_t)n * g.ldot + row] = h;
+                    } else if (g.epi == kEpiLinear) {
+                        g.outf[(size_t)row * g.ldof + n] = x + g.bias[n];
+                    } else if (g.epi == kEpiBackward) {
+                        const bf16 dz = __float2bfloat16_rn(x * dsilu(g.zprev[(size_t)row * g.ldz + n]));
+                        g.outb[(size_t)row * g.ldob + n] = dz;
+                        g.outt[(size_t)n * g.ldot + row] = dz;
+                    } else {
+                        g.outf[(size_t)row * g.ldof + n] = x;
+                    }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc_bar_arrive(&acc_empty[a]);
         }
     }
+    if (!ok) atomicOr(g.err, 1u);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_dealloc(tmem, tn);
+    tc_fence_after();
+    if (warp == 0) tc_dealloc(tmem, 2 * tn);
 }
 
 // Tensor map of a row-major BF16 matrix [rows][ld] whose first `cols` columns are the operand:
@@ -199,8 +211,8 @@ int tensor_map(CUtensorMap* map, const bf16* base, uint32_t rows, uint32_t cols,
     return ARBO_OK;
 }
 
-// Launches C = A B^T with the epilogue of g: 128 x 256 tiles when that still gives at least one
-// tile per SM, else 128 x 128. Returns a cudaError_t (invalid value when a tensor map cannot be
+// Launches C = A B^T with the epilogue of g on min(tiles, SMs) persistent CTAs: 128 x 256 tiles
+// when that still gives at least one tile per SM, else 128 x 128. Returns a cudaError_t (invalid value when a tensor map cannot be
 // built; the reason is then in arbo_last_error).
 int gemm_launch(const GemmArgs& g, cudaStream_t st, uint32_t num_sm)
 {
@@ -209,8 +221,8 @@ int gemm_launch(const GemmArgs& g, cudaStream_t st, uint32_t num_sm)
     CUtensorMap ma, mb;
     if (tensor_map(&ma, g.A, g.M, g.K, g.lda, kTileM) || tensor_map(&mb, g.B, g.N, g.K, g.ldb, tn))
         return (int)cudaErrorInvalidValue;
-    const dim3 grid(mt, (g.N + tn - 1) / tn);
-    k_gemm_tn<<<grid, 128, kGemmSmem, st>>>(ma, mb, g, tn);
+    const uint32_t tiles = mt * ((g.N + tn - 1) / tn);
+    k_gemm_tn<<<tiles < num_sm ? tiles : num_sm, 192, kGemmSmem, st>>>(ma, mb, g, tn);
     return (int)cudaGetLastError();
 }
 

@@ -118,6 +118,12 @@ __device__ __forceinline__ void tc_bar_expect_tx(unsigned long long* bar, uint32
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem(bar)), "r"(bytes) : "memory");
 }
 
+// Plain arrival (count 1) on an mbarrier.
+__device__ __forceinline__ void tc_bar_arrive(unsigned long long* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem(bar)) : "memory");
+}
+
 // Tiled TMA load of a 2-D box at element coordinates (x innermost, y) into shared memory,
 // completing on `bar`. x times the element size must be a multiple of 16 bytes.
 __device__ __forceinline__ void tc_tma_load_2d(void* dst, const CUtensorMap* map, int32_t x, int32_t y,
