@@ -111,24 +111,25 @@ __device__ __forceinline__ uint32_t human_comm(const uint32_t* __restrict__ nloc
     return c;
 }
 
-// Rare per-human path: a transition of an infected human or a death with rebirth.
+// Rare per-human path: a transition of an infected human or a death with rebirth. `when` is the
+// human's recovery age (status 2) or exposed age (status 1), already loaded by the caller.
 // Returns the new status byte, with bit 8 set when the human died (its age restarts at 0).
-__device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, int32_t dage, uint32_t t,
+__device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, int32_t dage, int32_t when, uint32_t t,
                                             const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ hcomm,
-                                            uint32_t P, const int32_t* n_exposed, const int32_t* n_recovery,
-                                            const uint8_t* n_strain, float* n_ple, int32_t* n_dage, uint8_t* n_imm,
-                                            uint32_t* infh, uint32_t* inc, const float* __restrict__ cdfh,
-                                            const uint32_t* __restrict__ minvh, uint32_t ah, Key key, Ctrl* ctrl)
+                                            uint32_t P, const uint8_t* n_strain, float* n_ple, int32_t* n_dage,
+                                            uint8_t* n_imm, uint32_t* infh, uint32_t* inc,
+                                            const float* __restrict__ cdfh, const uint32_t* __restrict__ minvh,
+                                            uint32_t ah, Key key, Ctrl* ctrl)
 {
     if (a < dage) {
         if (st == 2) {
-            if (n_recovery[i] < a) {
+            if (when < a) {
                 const uint32_t c = human_comm(nloc, hcomm, P, i);
                 counter_dec(&infh[n_strain[i] * P + c], ctrl);
                 return 0;
             }
         } else if (st == 1) {
-            if (n_exposed[i] < a) {
+            if (when < a) {
                 const uint32_t c = human_comm(nloc, hcomm, P, i);
                 const uint32_t s = n_strain[i];
                 atomicAdd(&inc[s * P + c], 1u);
@@ -174,6 +175,14 @@ __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32
         const int32_t dd[4] = {D[u].x, D[u].y, D[u].z, D[u].w};
         const uint32_t sw = SW[u];
         uint32_t nsw = sw;
+        // Exposed and infectious humans of the group: their exposed / recovery ages in one
+        // vector load each, so that only actual transitions take the slow path.
+        const uint32_t live = ~sw & 0x80808080u;  // bit 7 of a byte: not padding
+        const uint32_t b0 = sw & (live >> 7), b1 = (sw >> 1) & (live >> 7);
+        int4 E = make_int4(0, 0, 0, 0), R = E;
+        if (b0 & ~b1 & 0x01010101u) E = reinterpret_cast<const int4*>(d.n_exposed)[g];   // a byte == 1
+        if (b1 & ~b0 & 0x01010101u) R = reinterpret_cast<const int4*>(d.n_recovery)[g];  // a byte == 2
+        const int32_t ev[4] = {E.x, E.y, E.z, E.w}, rv[4] = {R.x, R.y, R.z, R.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t st = (sw >> (8 * k)) & 0xFFu;
@@ -181,10 +190,12 @@ __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32
                 a[k] -= 1;
                 continue;
             }
-            if (st == 0 && a[k] < dd[k]) continue;  // susceptible survivor: ageing only
-            const uint32_t res = human_slow(4 * g + k, st, a[k], dd[k], t, d.nloc, d.hcomm, d.P, d.n_exposed,
-                                            d.n_recovery, d.n_strain, d.n_ple, d.n_dage, d.n_imm, d.infh, d.inc,
-                                            d.cdfh, d.minvh, d.ah, key, d.ctrl);
+            const int32_t when = st == 1 ? ev[k] : rv[k];
+            if (a[k] < dd[k] && (st == 0 || ((st == 1 || st == 2) && !(when < a[k]))))
+                continue;  // survivor without a transition: ageing only
+            const uint32_t res = human_slow(4 * g + k, st, a[k], dd[k], when, t, d.nloc, d.hcomm, d.P, d.n_strain,
+                                            d.n_ple, d.n_dage, d.n_imm, d.infh, d.inc, d.cdfh, d.minvh, d.ah, key,
+                                            d.ctrl);
             if (res & 0x100u) a[k] = 0;
             nsw = (nsw & ~(0xFFu << (8 * k))) | ((res & 0xFFu) << (8 * k));
         }
