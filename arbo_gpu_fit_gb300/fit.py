@@ -36,6 +36,7 @@ class FitSetup:
     chains: int
     months: int
     info: dict = field(default_factory=dict)
+    replicates: int = 1
 
 
 def workload(population: str, seed: int = configs.DEFAULT_SEED) -> configs.Workload:
@@ -47,7 +48,7 @@ def workload(population: str, seed: int = configs.DEFAULT_SEED) -> configs.Workl
 
 
 def setup(population: str = "small", chains: int = 64, months: int = 120, seed: int = 11,
-          start: str = "near", step_fraction: float = STEP_FRACTION) -> FitSetup:
+          start: str = "near", step_fraction: float = STEP_FRACTION, replicates: int = 1) -> FitSetup:
     """start 'near': chains start within 5 % of the box width of the true vector, so that the
     comparison measures mixing rather than burn-in; 'spread': over the middle half of the box."""
     w = workload(population)
@@ -60,7 +61,7 @@ def setup(population: str = "small", chains: int = 64, months: int = 120, seed: 
     else:
         theta0 = lo + (hi - lo) * rng.uniform(0.25, 0.75, (chains, len(lo)))
     step = step_fraction * (hi - lo)
-    return FitSetup(w, obs, theta0, step, chains, months, {"population": population})
+    return FitSetup(w, obs, theta0, step, chains, months, {"population": population}, replicates)
 
 
 def summarize(chain: np.ndarray, minutes: float, burn: int) -> dict:
@@ -74,7 +75,7 @@ def summarize(chain: np.ndarray, minutes: float, burn: int) -> dict:
 
 
 def run_plain(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
-    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
     r = mcmc.run_plain(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
@@ -97,7 +98,7 @@ def train_surrogate(fs: FitSetup, runs: int, epochs: int, seed: int = 3, hidden:
 
 
 def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
-    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
     r = mcmc.run_delayed(m, iters, fs.theta0, lambda th: sur.loglik(th, fs.observed),
                          adapt=mcmc.StepAdapter(adapt_until))
     chain, flags = m.chain(iters)
@@ -111,7 +112,7 @@ def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_u
 
 
 def run_batched(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
-    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters)
+    m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
     r = mcmc.run_batched(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
@@ -123,15 +124,15 @@ def run_batched(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -
 
 def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt_until: int = 60,
             plain_iters: int = 20, train_runs: int = 4096, epochs: int = 60, seed: int = 11,
-            step_fraction: float = STEP_FRACTION) -> dict:
+            step_fraction: float = STEP_FRACTION, replicates: int = 1) -> dict:
     """Plain, batched and batched + surrogate (delayed acceptance) chains on one setup.
 
     Plain and batched produce bit-identical chains (the random streams are keyed; tested), so the
     plain chain's effective sample size for `iters` iterations is the batched chain's, and its
     time is plain_iters measured iterations scaled to `iters` (every iteration simulates every
     chain once). The first plain_iters states of both are compared here as well."""
-    fs = setup(population, chains=chains, seed=seed, step_fraction=step_fraction)
-    out = {"population": population, "step_fraction": step_fraction, "chains": chains, "iters": iters, "adapt_until": adapt_until,
+    fs = setup(population, chains=chains, seed=seed, step_fraction=step_fraction, replicates=replicates)
+    out = {"population": population, "step_fraction": step_fraction, "replicates": replicates, "chains": chains, "iters": iters, "adapt_until": adapt_until,
            "theta_true": THETA_TRUE.tolist()}
     b = run_batched(fs, iters, adapt_until=adapt_until)
     p = run_plain(fs, plain_iters, adapt_until=adapt_until)
@@ -172,13 +173,15 @@ def main(argv=None):
     ap.add_argument("--train-runs", type=int, default=4096)
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--step-fraction", type=float, default=STEP_FRACTION)
+    ap.add_argument("--replicates", type=int, default=1, help="simulations per proposal (log-mean-exp)")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     _native.check(_native.load().arbo_set_device(a.device))
     t0 = time.perf_counter()
     r = compare(a.population, chains=a.chains, iters=a.iters, adapt_until=a.adapt, plain_iters=a.plain_iters,
-                train_runs=a.train_runs, epochs=a.epochs, step_fraction=a.step_fraction)
+                train_runs=a.train_runs, epochs=a.epochs, step_fraction=a.step_fraction,
+                replicates=a.replicates)
     r["total_s"] = time.perf_counter() - t0
     text = json.dumps(r, indent=1)
     if a.out:
