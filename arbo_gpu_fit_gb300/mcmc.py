@@ -119,6 +119,7 @@ class MCMC:
     def propose(self, it: int) -> np.ndarray:
         out = np.zeros((self.C, self.D), np.float64)
         check(self._lib.arbo_mcmc_propose(self._h, int(it), _dp(out), None))
+        self._last_prop = out
         return out
 
     def check_params(self, theta: np.ndarray) -> np.ndarray:
@@ -236,6 +237,8 @@ def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simul
     sims = sims if sims is not None else m.make_sims(m.R)
     t0 = time.perf_counter()
     start(m, theta0, sims)
+    if on_iter:
+        on_iter(0)
     sim_s = 0.0
     for it in range(1, iters):
         prop = m.propose(it)
@@ -264,6 +267,8 @@ def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Sim
     batch = batch if batch is not None else Batch(sims)
     t0 = time.perf_counter()
     start(m, theta0, sims, batch)
+    if on_iter:
+        on_iter(0)
     sim_s = 0.0
     for it in range(1, iters):
         prop = m.propose(it)
@@ -300,6 +305,8 @@ def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np
     with Batch(sims) as b0:
         start(m, theta0, sims, b0)
     m.set_screen(surrogate(theta0), surrogate(theta0))
+    if on_iter:
+        on_iter(0)
     sim_s, simulated = 0.0, m.C * m.R
     batches = {}
     try:
@@ -370,3 +377,83 @@ def ess(samples: np.ndarray) -> np.ndarray:
             tau += 2 * pair
         out[d] = m2 * n / max(tau, 1e-12)
     return out
+
+
+# -- output files in the reference's formats (cpp/MCMC.cpp:383-484) --------------------------------
+
+def _fmt(x: float) -> str:
+    return repr(float(x))
+
+
+def write_priors(odir: str, box=None) -> str:
+    """MCMC_priors.csv as MCMC::writePriors writes it: one row per parameter with the prior's name
+    and parameters (here uniform on the box, printed like the reference's "(name = value;...)")."""
+    import os
+
+    box = box if box is not None else configs.PRIOR_BOX
+    path = os.path.join(odir, "MCMC_priors.csv")
+    with open(path, "w") as f:
+        f.write("PARAMETER_NAME,PRIOR_DISTRIBUTION,PARAMETERS")
+        for name, lo, hi in box:
+            f.write(f"\n{name},Uniform,(lower = {lo:f};upper = {hi:f})")
+    return path
+
+
+def write_chain(odir: str, chain: np.ndarray, logpost: np.ndarray, chain_index: int = 0, box=None) -> str:
+    """MCMC.csv as MCMC::writeChain writes it step by step: `step,logLikelihood,<params>` with the
+    accepted state of every step. chain: [iters, D] states of one chain; logpost: [iters] the
+    log-posterior of those states (the reference writes the last accepted log-likelihood).
+    Chains other than the first get their own file MCMC_<k>.csv."""
+    import os
+
+    box = box if box is not None else configs.PRIOR_BOX
+    path = os.path.join(odir, "MCMC.csv" if chain_index == 0 else f"MCMC_{chain_index}.csv")
+    with open(path, "w") as f:
+        f.write("step,logLikelihood" + "".join("," + b[0] for b in box))
+        for it in range(chain.shape[0]):
+            f.write(f"\n{it},{_fmt(logpost[it])}" + "".join("," + _fmt(v) for v in chain[it]))
+    return path
+
+
+def write_candidates(odir: str, candidates: np.ndarray, loglik: np.ndarray, accepted: np.ndarray,
+                     chain_index: int = 0, box=None) -> str:
+    """MCMC_candidates.csv as MCMC::writeCandidates writes it: `step,logLikelihood,<params>,accepted`
+    for every proposal of one chain."""
+    import os
+
+    box = box if box is not None else configs.PRIOR_BOX
+    path = os.path.join(odir, "MCMC_candidates.csv" if chain_index == 0 else f"MCMC_candidates_{chain_index}.csv")
+    with open(path, "w") as f:
+        f.write("step,logLikelihood" + "".join("," + b[0] for b in box) + ",accepted")
+        for it in range(candidates.shape[0]):
+            f.write(f"\n{it},{_fmt(loglik[it])}" + "".join("," + _fmt(v) for v in candidates[it]) +
+                    f",{int(accepted[it])}")
+    return path
+
+
+class ChainRecorder:
+    """on_iter callback of the drivers (called with 0 after the initial states are evaluated, then
+    after every iteration) that keeps every chain's proposals, their log-likelihoods and accept
+    flags for write_candidates, and the log posterior of the current states for write_chain (the
+    states themselves are recorded on the device, MCMC.chain)."""
+
+    def __init__(self, m: "MCMC"):
+        self.m = m
+        self.logpost, self.loglik, self.props = [], [], []
+
+    def __call__(self, it: int) -> None:
+        st = self.m.state()
+        self.logpost.append(st["logpost"].copy())
+        if it == 0:
+            self.loglik.append(st["logpost"].copy())
+            self.props.append(st["theta"].copy())
+        else:
+            self.loglik.append(st["loglik"].copy())
+            self.props.append(self.m._last_prop.copy())
+
+    def write(self, odir: str, chain_index: int = 0) -> None:
+        states, flags = self.m.chain(len(self.logpost))
+        lp = np.array(self.logpost)
+        write_chain(odir, states[:, chain_index], lp[:, chain_index], chain_index)
+        write_candidates(odir, np.array(self.props)[:, chain_index], np.array(self.loglik)[:, chain_index],
+                         flags[:, chain_index], chain_index)

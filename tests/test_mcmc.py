@@ -54,3 +54,20 @@ def test_serial_replay_is_deterministic_and_moves():
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.all(np.isfinite(a[2]))
     assert np.all(a[0][0] == theta0)
+
+
+def test_output_files_in_the_reference_formats(tmp_path):
+    from arbo_gpu_fit_gb300 import mcmc
+
+    p = mcmc.write_priors(str(tmp_path))
+    lines = open(p).read().split("\n")
+    assert lines[0] == "PARAMETER_NAME,PRIOR_DISTRIBUTION,PARAMETERS" and len(lines) == 7
+    assert lines[1].startswith("nmBitingSuccess,Uniform,(lower = 0.100000;upper = 1.000000)")
+    chain = np.arange(18, dtype=float).reshape(3, 6) / 10
+    p = mcmc.write_chain(str(tmp_path), chain, np.array([-5.0, -4.5, -4.5]))
+    lines = open(p).read().split("\n")
+    assert lines[0] == "step,logLikelihood,nmBitingSuccess,mnBitingSuccess,localFraction,seasonAmp,seasonPhase,reportingRate"
+    assert lines[2].split(",")[:3] == ["1", "-4.5", "0.6"] and len(lines) == 4
+    p = mcmc.write_candidates(str(tmp_path), chain, np.array([-5.0, -4.0, -9.0]), np.array([1, 1, 0]))
+    lines = open(p).read().split("\n")
+    assert lines[0].endswith(",accepted") and lines[3].endswith(",0")

@@ -70,3 +70,21 @@ def test_delayed_acceptance(gpu):
     st = sel.state()
     assert st["accepted"].sum() <= st["passed"].sum() < 4 * 7
     assert run["simulations"] == 4 + int(st["passed"].sum())
+
+
+def test_chain_files(gpu, tmp_path):
+    w, obs, theta0 = setup(chains=2, T=60, months=2)
+    m = mcmc.MCMC(w, obs, 2, STEP, seed=4, max_iters=5)
+    rec = mcmc.ChainRecorder(m)
+    mcmc.run_batched(m, 5, theta0, on_iter=rec)
+    rec.write(str(tmp_path), 0)
+    rec.write(str(tmp_path), 1)
+    chain, flags = m.chain(5)
+    rows = [l.split(",") for l in open(tmp_path / "MCMC_1.csv").read().split("\n")[1:]]
+    assert len(rows) == 5 and np.allclose([float(x) for x in rows[-1][2:]], chain[-1, 1])
+    cand = [l.split(",") for l in open(tmp_path / "MCMC_candidates.csv").read().split("\n")[1:]]
+    assert [int(r[-1]) for r in cand] == [int(f) for f in flags[:, 0]]
+    # An accepted candidate becomes the chain's state.
+    for it in range(1, 5):
+        if flags[it, 0]:
+            assert np.allclose([float(x) for x in cand[it][2:-1]], chain[it, 0])
