@@ -411,9 +411,9 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         size_t bytes;
     };
     std::vector<Item> items = {
-        {(void**)&d.n_age, Np * 4}, {(void**)&d.n_dage, Np * 4}, {(void**)&d.n_status, Np}, {(void**)&d.n_exposed, Np * 4},
+        {(void**)&d.n_born, Np * 4}, {(void**)&d.n_dtime, Np * 4}, {(void**)&d.n_status, Np}, {(void**)&d.n_exposed, Np * 4},
         {(void**)&d.n_recovery, Np * 4}, {(void**)&d.n_ple, Np * 4}, {(void**)&d.n_strain, Np}, {(void**)&d.n_imm, Np},
-        {(void**)&d.m_age, Mp * 4}, {(void**)&d.m_dage, Mp * 4}, {(void**)&d.m_state, Mp}, {(void**)&d.m_exposed, Mp * 4},
+        {(void**)&d.m_born, Mp * 4}, {(void**)&d.m_dtime, Mp * 4}, {(void**)&d.m_state, Mp}, {(void**)&d.m_exposed, Mp * 4},
         {(void**)&d.m_ple, Mp * 4}, {(void**)&d.m_strain, Mp}, {(void**)&d.ledger, (size_t)d.tiles * 4},
         {(void**)&d.nloc, (P + 1) * 4}, {(void**)&d.mloc, (P + 1) * 4}, {(void**)&d.nsize, P * 4},
         {(void**)&d.msize, P * 4}, {(void**)&d.tcomm, (size_t)d.tiles * 4}, {(void**)&d.csr_loc, (P + 1) * 4},
@@ -773,24 +773,56 @@ static int census_ptr(arbo_sim* s, arbo_census_field f, void** ptr, size_t* coun
     const Dev& d = s->d;
     *packed = 0;
     switch (f) {
-    case ARBO_CENSUS_N_AGE: *ptr = d.n_age; *elem = 4; break;
+    case ARBO_CENSUS_N_AGE: *ptr = d.n_born; *elem = 4; *packed = 3; break;
     case ARBO_CENSUS_N_EXPOSED: *ptr = d.n_exposed; *elem = 4; break;
     case ARBO_CENSUS_N_IMMUNITY: *ptr = d.n_imm; *elem = 1; break;
     case ARBO_CENSUS_N_STATUS: *ptr = d.n_status; *elem = 1; break;
     case ARBO_CENSUS_N_PLE: *ptr = d.n_ple; *elem = 4; break;
     case ARBO_CENSUS_N_RECOVERY: *ptr = d.n_recovery; *elem = 4; break;
     case ARBO_CENSUS_N_STRAIN: *ptr = d.n_strain; *elem = 1; break;
-    case ARBO_CENSUS_N_DEATH_AGE: *ptr = d.n_dage; *elem = 4; break;
-    case ARBO_CENSUS_M_AGE: *ptr = d.m_age; *elem = 4; break;
+    case ARBO_CENSUS_N_DEATH_AGE: *ptr = d.n_dtime; *elem = 4; *packed = 3; break;
+    case ARBO_CENSUS_M_AGE: *ptr = d.m_born; *elem = 4; *packed = 3; break;
     case ARBO_CENSUS_M_DEAD: *ptr = d.m_state; *elem = 1; *packed = 1; break;
     case ARBO_CENSUS_M_EXPOSED: *ptr = d.m_exposed; *elem = 4; break;
     case ARBO_CENSUS_M_STATUS: *ptr = d.m_state; *elem = 1; *packed = 2; break;
     case ARBO_CENSUS_M_PLE: *ptr = d.m_ple; *elem = 4; break;
     case ARBO_CENSUS_M_STRAIN: *ptr = d.m_strain; *elem = 1; break;
-    case ARBO_CENSUS_M_DEATH_AGE: *ptr = d.m_dage; *elem = 4; break;
+    case ARBO_CENSUS_M_DEATH_AGE: *ptr = d.m_dtime; *elem = 4; *packed = 3; break;
     default: return fail(ARBO_ERR_INVALID, "unknown census field");
     }
     *count = f <= ARBO_CENSUS_N_DEATH_AGE ? d.N : d.M;
+    return ARBO_OK;
+}
+
+// Ages and death ages derived from the birth and death times: a live agent's age is now - born;
+// a dead mosquito slot keeps the age at which it died, max(dtime, max(born, 0) + 1) - born (it
+// died in the first step after its birth, at time max(born, 0), that reached its death time); a
+// slot dead since initialisation (dtime INT_MIN) reads age 0 and death age 0.
+static int census_derived(arbo_sim* s, arbo_census_field f, int32_t* out, size_t count, void* stream)
+{
+    const Dev& d = s->d;
+    uint32_t err = 0, now = 0;
+    int e = arbo_sim_status(s, stream, &err, &now);
+    if (e) return e;
+    const bool human = f == ARBO_CENSUS_N_AGE || f == ARBO_CENSUS_N_DEATH_AGE;
+    std::vector<int32_t> born(count), dtime(count);
+    std::vector<uint8_t> state;
+    if ((e = copy_out(s, born.data(), human ? d.n_born : d.m_born, count * 4, stream))) return e;
+    if ((e = copy_out(s, dtime.data(), human ? d.n_dtime : d.m_dtime, count * 4, stream))) return e;
+    if (f == ARBO_CENSUS_M_AGE) {
+        state.resize(count);
+        if ((e = copy_out(s, state.data(), d.m_state, count, stream))) return e;
+    }
+    const int32_t tn = (int32_t)now;
+    for (size_t i = 0; i < count; ++i) {
+        const int32_t b = born[i], x = dtime[i];
+        if (f == ARBO_CENSUS_N_AGE) out[i] = tn - b;
+        else if (f == ARBO_CENSUS_M_AGE) {
+            if (!(state[i] & kDead)) out[i] = tn - b;
+            else if (x == INT_MIN) out[i] = 0;
+            else out[i] = std::max(x, std::max(b, 0) + 1) - b;
+        } else out[i] = x == INT_MAX ? INT_MAX : x == INT_MIN ? 0 : x - b;
+    }
     return ARBO_OK;
 }
 
@@ -803,6 +835,7 @@ int arbo_sim_get_census(arbo_sim* s, arbo_census_field f, void* host, size_t byt
     int e = census_ptr(s, f, &ptr, &count, &elem, &packed);
     if (e) return e;
     if (bytes != count * elem) return fail(ARBO_ERR_INVALID, "census size mismatch: expected " + std::to_string(count * elem));
+    if (packed == 3) return census_derived(s, f, (int32_t*)host, count, stream);
     e = copy_out(s, host, ptr, bytes, stream);
     if (e || !packed) return e;
     uint8_t* h = (uint8_t*)host;
@@ -819,6 +852,8 @@ int arbo_sim_set_census(arbo_sim* s, arbo_census_field f, const void* host, size
     int e = census_ptr(s, f, &ptr, &count, &elem, &packed);
     if (e) return e;
     if (bytes != count * elem) return fail(ARBO_ERR_INVALID, "census size mismatch: expected " + std::to_string(count * elem));
+    if (packed == 3)
+        return fail(ARBO_ERR_INVALID, "ages and death ages are derived from birth and death times and cannot be set");
     CUDA_TRY(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
     if (!packed) {

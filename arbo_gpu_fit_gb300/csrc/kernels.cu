@@ -2,7 +2,8 @@
 //
 // One step is three launches (captured in a CUDA graph by the host):
 //   k_demog   human and mosquito demographic passes over the whole census (HBM stream:
-//             read age, death age, status; write age), per-tile mosquito recruitment,
+//             read status and death time; ages are birth times, so a survivor without a
+//             transition writes nothing), per-tile mosquito recruitment,
 //             counter deltas; replaces nBlockBirthDeath + resetIncidence + mBlockBirthDeath
 //             (cpp/ndemographic.cu:32-120, cpp/mdemographic.cu:22-150).
 //   k_foi     per (serotype, community): the series row of the next time point, then the
@@ -111,17 +112,19 @@ __device__ __forceinline__ uint32_t human_comm(const uint32_t* __restrict__ nloc
     return c;
 }
 
-// Rare per-human path: a transition of an infected human or a death with rebirth. `when` is the
-// human's recovery age (status 2) or exposed age (status 1), already loaded by the caller.
-// Returns the new status byte, with bit 8 set when the human died (its age restarts at 0).
-__device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, int32_t dage, int32_t when, uint32_t t,
-                                            const uint32_t* __restrict__ nloc, const uint32_t* __restrict__ hcomm,
-                                            uint32_t P, const uint8_t* n_strain, float* n_ple, int32_t* n_dage,
-                                            uint8_t* n_imm, uint32_t* infh, uint32_t* inc,
-                                            const float* __restrict__ cdfh, const uint32_t* __restrict__ minvh,
-                                            uint32_t ah, Key key, Ctrl* ctrl)
+// Rare per-human path, in the step that reaches time tn: a transition of an infected human or a
+// death with rebirth. `when` is the human's recovery age (status 2) or exposed age (status 1)
+// and `born` its birth time, both loaded by the caller for an infected human (its age is
+// tn - born). Returns the new status byte.
+__device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t tn, int32_t dtime, int32_t born,
+                                            int32_t when, uint32_t t, const uint32_t* __restrict__ nloc,
+                                            const uint32_t* __restrict__ hcomm, uint32_t P, const uint8_t* n_strain,
+                                            float* n_ple, int32_t* n_born, int32_t* n_dtime, uint8_t* n_imm,
+                                            uint32_t* infh, uint32_t* inc, const float* __restrict__ cdfh,
+                                            const uint32_t* __restrict__ minvh, uint32_t ah, Key key, Ctrl* ctrl)
 {
-    if (a < dage) {
+    if (tn < dtime) {
+        const int32_t a = tn - born;
         if (st == 2) {
             if (when < a) {
                 const uint32_t c = human_comm(nloc, hcomm, P, i);
@@ -146,24 +149,28 @@ __device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t a, 
     const U4 r = draw4(key, kHumanRebirth, i >> 2, t);
     const float ple = u01(r.v[i & 3]);
     n_ple[i] = ple;
-    n_dage[i] = death_age_inv(cdfh, minvh, ah, ple, 65536.0f);
+    n_born[i] = tn;
+    n_dtime[i] = death_time(tn, death_age_inv(cdfh, minvh, ah, ple, 65536.0f));
     n_imm[i] = 0;
-    return 0x100u;
+    return 0;
 }
 
+// Human pass over groups of four (cpp/ndemographic.cu:32-105): ageing is implicit in the birth
+// times; a human dies when the new time reaches its death time, and an exposed or infectious one
+// changes status when its exposed or recovery age falls below its new age.
 template <int U>
 __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32_t g0, uint32_t stride, uint32_t t)
 {
-    int4 A[U], D[U];
+    int4 D[U];
     uint32_t SW[U];
     bool ok[U];
+    const int32_t tn = (int32_t)t + 1;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const uint32_t g = g0 + u * stride;
         ok[u] = g < d.nvec;
         if (ok[u]) {
-            A[u] = reinterpret_cast<const int4*>(d.n_age)[g];
-            D[u] = __ldcs(reinterpret_cast<const int4*>(d.n_dage) + g);
+            D[u] = __ldcs(reinterpret_cast<const int4*>(d.n_dtime) + g);
             SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.n_status) + g);
         }
     }
@@ -171,35 +178,34 @@ __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32
     for (int u = 0; u < U; ++u) {
         if (!ok[u]) continue;
         const uint32_t g = g0 + u * stride;
-        int32_t a[4] = {A[u].x + 1, A[u].y + 1, A[u].z + 1, A[u].w + 1};
         const int32_t dd[4] = {D[u].x, D[u].y, D[u].z, D[u].w};
         const uint32_t sw = SW[u];
-        uint32_t nsw = sw;
-        // Exposed and infectious humans of the group: their exposed / recovery ages in one
-        // vector load each, so that only actual transitions take the slow path.
+        // A death in the group, or an exposed or infectious human in it, takes the slow path.
+        const bool dies = tn >= dd[0] || tn >= dd[1] || tn >= dd[2] || tn >= dd[3];
         const uint32_t live = ~sw & 0x80808080u;  // bit 7 of a byte: not padding
         const uint32_t b0 = sw & (live >> 7), b1 = (sw >> 1) & (live >> 7);
-        int4 E = make_int4(0, 0, 0, 0), R = E;
+        const uint32_t inf = (b0 ^ b1) & 0x01010101u;  // bytes with status 1 or 2
+        if (!dies && !inf) continue;
+        // Exposed and infectious humans: their exposed / recovery ages and birth times in one
+        // vector load each, so that only actual transitions take the slow path.
+        int4 E = make_int4(0, 0, 0, 0), R = E, B = E;
+        if (inf) B = reinterpret_cast<const int4*>(d.n_born)[g];
         if (b0 & ~b1 & 0x01010101u) E = reinterpret_cast<const int4*>(d.n_exposed)[g];   // a byte == 1
         if (b1 & ~b0 & 0x01010101u) R = reinterpret_cast<const int4*>(d.n_recovery)[g];  // a byte == 2
-        const int32_t ev[4] = {E.x, E.y, E.z, E.w}, rv[4] = {R.x, R.y, R.z, R.w};
+        const int32_t ev[4] = {E.x, E.y, E.z, E.w}, rv[4] = {R.x, R.y, R.z, R.w}, bv[4] = {B.x, B.y, B.z, B.w};
+        uint32_t nsw = sw;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const uint32_t st = (sw >> (8 * k)) & 0xFFu;
-            if (st == kPad) {
-                a[k] -= 1;
-                continue;
-            }
+            if (st == kPad) continue;
             const int32_t when = st == 1 ? ev[k] : rv[k];
-            if (a[k] < dd[k] && (st == 0 || ((st == 1 || st == 2) && !(when < a[k]))))
-                continue;  // survivor without a transition: ageing only
-            const uint32_t res = human_slow(4 * g + k, st, a[k], dd[k], when, t, d.nloc, d.hcomm, d.P, d.n_strain,
-                                            d.n_ple, d.n_dage, d.n_imm, d.infh, d.inc, d.cdfh, d.minvh, d.ah, key,
-                                            d.ctrl);
-            if (res & 0x100u) a[k] = 0;
+            if (tn < dd[k] && (st == 0 || ((st == 1 || st == 2) && !(when < tn - bv[k]))))
+                continue;  // survivor without a transition
+            const uint32_t res = human_slow(4 * g + k, st, tn, dd[k], bv[k], when, t, d.nloc, d.hcomm, d.P,
+                                            d.n_strain, d.n_ple, d.n_born, d.n_dtime, d.n_imm, d.infh, d.inc, d.cdfh,
+                                            d.minvh, d.ah, key, d.ctrl);
             nsw = (nsw & ~(0xFFu << (8 * k))) | ((res & 0xFFu) << (8 * k));
         }
-        reinterpret_cast<int4*>(d.n_age)[g] = make_int4(a[0], a[1], a[2], a[3]);
         if (nsw != sw) reinterpret_cast<unsigned int*>(d.n_status)[g] = nsw;
     }
 }
@@ -266,21 +272,20 @@ __device__ __forceinline__ uint32_t keep_low(uint32_t mask, uint32_t m)
     return (uint32_t)(lut >> (4 * mask)) & 0xFu;
 }
 
-// One warp, tiles 4q..4q+3; lane l holds slots 4l..4l+3 of each tile. Per tile: ageing and
-// deaths, the birth quota (cpp/mdemographic.cu:104-129) from the carried dead count, rebirth of
+// One warp, tiles 4q..4q+3; lane l holds slots 4l..4l+3 of each tile. Per tile: deaths (an
+// alive slot dies when the new time reaches its death time), the birth quota (cpp/mdemographic.cu:104-129) from the carried dead count, rebirth of
 // the lowest-index dead slots, the net change of each community's alive count. The quota draws
 // of the four tiles come from one Philox call; the r-th reborn slot of tile b takes component
 // r&3 of the call keyed (b, t, r>>2). Per-tile counts of the four tiles travel packed in the
 // four bytes of one word (at most 128 per tile), so one warp reduction or scan serves all four.
-// Slot-owner lanes age their slots, store the aged ages, clear the state bytes of their reborn
-// slots and post each reborn slot's offset under its rank; one lane per group of four reborn
-// slots then draws the group, and one lane per reborn slot writes the newborn's age, PLE and
-// death age.
+// Slot-owner lanes test their slots, clear the state bytes of their reborn slots and post each
+// reborn slot's offset under its rank; one lane per group of four reborn slots then draws the
+// group, and one lane per reborn slot writes the newborn's PLE, birth time and death time.
 __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, uint32_t q, uint32_t lane, uint32_t t,
-                                                   QuadSmem& sm, uint32_t (&SW)[kQuad], int4 (&A)[kQuad],
-                                                   const int4 (&D)[kQuad])
+                                                   QuadSmem& sm, uint32_t (&SW)[kQuad], const int4 (&D)[kQuad])
 {
     const uint32_t b0 = q * kQuad;
+    const int32_t tn = (int32_t)t + 1;
     const uint32_t bl = b0 + lane;
     const bool tile_lane = lane < kQuad && bl < d.tiles;
     const int32_t led = tile_lane ? d.ledger[bl] : 0;
@@ -301,15 +306,13 @@ __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, 
         if (b0 + u == d.tiles - 1) dead4 &= ~__vcmpeq4(sw, 0xFFFFFFFFu);
         const uint32_t al0 = (alive4 >> 7) & 1u, al1 = (alive4 >> 15) & 1u, al2 = (alive4 >> 23) & 1u,
                        al3 = alive4 >> 31;
-        int32_t a[4] = {A[u].x + (int32_t)al0, A[u].y + (int32_t)al1, A[u].z + (int32_t)al2, A[u].w + (int32_t)al3};
-        const uint32_t dim = (al0 & (uint32_t)(a[0] >= D[u].x)) | ((al1 & (uint32_t)(a[1] >= D[u].y)) << 1) |
-                             ((al2 & (uint32_t)(a[2] >= D[u].z)) << 2) | ((al3 & (uint32_t)(a[3] >= D[u].w)) << 3);
+        const uint32_t dim = (al0 & (uint32_t)(tn >= D[u].x)) | ((al1 & (uint32_t)(tn >= D[u].y)) << 1) |
+                             ((al2 & (uint32_t)(tn >= D[u].z)) << 2) | ((al3 & (uint32_t)(tn >= D[u].w)) << 3);
         const uint32_t dm = nibble7(dead4) | dim;
         const uint32_t stat4 = sw & 0x03030303u;
         uint32_t rm = nibble7(((stat4 | (stat4 >> 1)) & (alive4 >> 7)) << 7);
         uint32_t ns = sw | (((dim * 0x00204081u) & 0x01010101u) << 7);
         const uint32_t g = (b0 + u) * 32 + lane;
-        if (alive4) reinterpret_cast<int4*>(d.m_age)[g] = make_int4(a[0], a[1], a[2], a[3]);
         // Rare: deaths of infectious mosquitoes and latent-to-infectious transitions.
         while (rm) {
             const int k = __ffs(rm) - 1;
@@ -319,8 +322,7 @@ __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, 
             if (st & kDead) {
                 if ((st & 3u) == 2u) mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, -1, d.ctrl);
             } else if ((st & 3u) == 1u) {
-                const int32_t ak = k == 0 ? a[0] : k == 1 ? a[1] : k == 2 ? a[2] : a[3];
-                if (d.m_exposed[i] < ak) {
+                if (d.m_exposed[i] < tn - d.m_born[i]) {
                     ns = (ns & ~(0x3u << (8 * k))) | (2u << (8 * k));
                     mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, +1, d.ctrl);
                 }
@@ -432,8 +434,8 @@ __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, 
         const uint32_t c = r & 3u;
         const float ple = u01(c == 0 ? v4.x : c == 1 ? v4.y : c == 2 ? v4.z : v4.w);
         d.m_ple[i] = ple;
-        d.m_dage[i] = death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f);
-        d.m_age[i] = 0;
+        d.m_born[i] = tn;
+        d.m_dtime[i] = death_time(tn, death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f));
     }
     __syncwarp();
 }
@@ -444,21 +446,19 @@ __device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key,
 {
     const uint32_t b0 = q * kQuad;
     uint32_t SW[kQuad];
-    int4 A[kQuad], D[kQuad];
+    int4 D[kQuad];
 #pragma unroll
     for (uint32_t u = 0; u < kQuad; ++u) {
         if (b0 + u < d.tiles) {
             const uint32_t g = (b0 + u) * 32 + lane;
             SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.m_state) + g);
-            A[u] = reinterpret_cast<const int4*>(d.m_age)[g];
-            D[u] = __ldcs(reinterpret_cast<const int4*>(d.m_dage) + g);
+            D[u] = __ldcs(reinterpret_cast<const int4*>(d.m_dtime) + g);
         } else {
             SW[u] = 0xFFFFFFFFu;
-            A[u] = make_int4(0, 0, 0, 0);
-            D[u] = A[u];
+            D[u] = make_int4(0, 0, 0, 0);
         }
     }
-    mosquito_quad_core(d, key, q, lane, t, sm, SW, A, D);
+    mosquito_quad_core(d, key, q, lane, t, sm, SW, D);
 }
 
 // ------------------------------------------------------------------ TMA-staged pipeline
@@ -466,8 +466,7 @@ __device__ __forceinline__ void demog_mosquito_quad(const Dev& d, const Key key,
 // One warp's double buffer of quad census words, filled by bulk asynchronous copies.
 struct MosqStage {
     uint32_t state[kQuad * 32];
-    int4 age[kQuad * 32];
-    int4 dage[kQuad * 32];
+    int4 dtime[kQuad * 32];
 };
 struct TmaWarpSmem {
     MosqStage stage[2];
@@ -526,10 +525,9 @@ __device__ __forceinline__ void issue_quad(const Dev& d, uint32_t q, MosqStage& 
     const uint32_t nt = min(kQuad, d.tiles - b0);
     // Order the warp's earlier generic reads of this buffer before the asynchronous writes.
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(bar, nt * kTile * 9);
+    mbar_expect_tx(bar, nt * kTile * 5);
     bulk_load(st.state, d.m_state + (size_t)b0 * kTile, nt * kTile, bar);
-    bulk_load(st.age, d.m_age + (size_t)b0 * kTile, nt * kTile * 4, bar);
-    bulk_load(st.dage, d.m_dage + (size_t)b0 * kTile, nt * kTile * 4, bar);
+    bulk_load(st.dtime, d.m_dtime + (size_t)b0 * kTile, nt * kTile * 4, bar);
 }
 
 // Persistent demographic pass with TMA staging. Every warp first walks chunks of 32*U human
@@ -574,21 +572,19 @@ __global__ void __launch_bounds__(128, 4) k_demog_tma(Dev d, uint32_t koff)
         const MosqStage& st = ws.stage[sidx];
         const uint32_t b0 = q * kQuad;
         uint32_t SW[kQuad];
-        int4 A[kQuad], D[kQuad];
+        int4 D[kQuad];
 #pragma unroll
         for (uint32_t u = 0; u < kQuad; ++u) {
             if (b0 + u < d.tiles) {
                 SW[u] = st.state[u * 32 + lane];
-                A[u] = st.age[u * 32 + lane];
-                D[u] = st.dage[u * 32 + lane];
+                D[u] = st.dtime[u * 32 + lane];
             } else {
                 SW[u] = 0xFFFFFFFFu;
-                A[u] = make_int4(0, 0, 0, 0);
-                D[u] = A[u];
+                D[u] = make_int4(0, 0, 0, 0);
             }
         }
         __syncwarp();  // every lane has its words before the buffer is refilled next iteration
-        mosquito_quad_core(d, key, q, lane, t, ws.qs, SW, A, D);
+        mosquito_quad_core(d, key, q, lane, t, ws.qs, SW, D);
     }
     griddep_launch_dependents();
 }
@@ -792,12 +788,14 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
 
 // ------------------------------------------------------------------ infection draws
 
-__device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r)
+// Infection of human i in step t, after the demographic pass of the step: its age is t + 1 - born.
+__device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r, uint32_t t)
 {
     d.n_status[i] = 1;
     d.n_strain[i] = (uint8_t)s;
     d.n_imm[i] = (uint8_t)(d.n_imm[i] | (1u << s));
-    const int32_t ex = (int32_t)resolve(__fadd_rn((float)d.n_age[i], d.nExposed), r.v[0]);
+    const int32_t age = (int32_t)t + 1 - d.n_born[i];
+    const int32_t ex = (int32_t)resolve(__fadd_rn((float)age, d.nExposed), r.v[0]);
     d.n_exposed[i] = ex;
     d.n_recovery[i] = (int32_t)resolve(__fadd_rn((float)ex, d.recovery), r.v[1]);
 }
@@ -1018,7 +1016,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 const uint32_t pl = __ffs(bal) - 1;
                 if (lane == pl) {
                     d.winh[i] = okey;
-                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a));
+                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t);
                 }
                 __syncwarp();
                 left -= 1;
@@ -1053,7 +1051,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 const uint32_t e = 4 * idx + q;
                 if (e >= k) break;
                 if (__ldcg(&d.winh[tg[q]]) == order_key(hiword, j, 0, e))
-                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e));
+                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t);
             }
         } else {
             const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
@@ -1063,7 +1061,8 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
                 d.m_state[slot] = 1;
                 d.m_strain[slot] = (uint8_t)sm;
-                d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)d.m_age[slot], d.mExposed), r.v[idx & 3]);
+                const int32_t age = (int32_t)t + 1 - d.m_born[slot];
+                d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)age, d.mExposed), r.v[idx & 3]);
             }
         }
     }
@@ -1194,8 +1193,8 @@ __global__ void k_init_humans(Dev d)
     if (j >= d.nvec * 4) return;
     if (j >= d.N) {
         d.n_status[j] = kPad;
-        d.n_age[j] = 0;
-        d.n_dage[j] = 0;
+        d.n_born[j] = 0;
+        d.n_dtime[j] = INT_MAX;
         d.n_ple[j] = 0.0f;
         d.n_strain[j] = 0;
         d.n_imm[j] = 0;
@@ -1216,9 +1215,9 @@ __global__ void k_init_humans(Dev d)
     uint32_t imm = 0;
     for (uint32_t s = 0; s < d.S; ++s)
         if (u01(dr[3 + s]) < d.seroPrev) imm |= 1u << s;
-    d.n_age[j] = age;
+    d.n_born[j] = -age;  // age `age` at time 0
     d.n_ple[j] = ple;
-    d.n_dage[j] = death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f);
+    d.n_dtime[j] = death_time(-age, death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f));
     d.n_status[j] = 0;
     d.n_strain[j] = 0;
     d.n_imm[j] = (uint8_t)imm;
@@ -1241,8 +1240,8 @@ __global__ void k_init_mosquitoes(Dev d)
         const uint32_t i = 4 * (b * 32 + lane) + k;
         if (i >= d.M) {
             d.m_state[i] = kPad;
-            d.m_age[i] = 0;
-            d.m_dage[i] = 0;
+            d.m_born[i] = 0;
+            d.m_dtime[i] = INT_MIN;
             d.m_ple[i] = 0.0f;
             d.m_strain[i] = 0;
             d.m_exposed[i] = 0;
@@ -1253,9 +1252,9 @@ __global__ void k_init_mosquitoes(Dev d)
         d.m_exposed[i] = 0;
         if (!(u01(r.v[0]) < alive_p)) {
             d.m_state[i] = kDead;
-            d.m_age[i] = 0;
+            d.m_born[i] = 0;
             d.m_ple[i] = 0.0f;
-            d.m_dage[i] = 0;
+            d.m_dtime[i] = INT_MIN;  // never alive: age 0, death age 0
             ndead += 1;
             atomicSub(&d.mcnt[slot_comm(d, c0, i)], 1u);
         } else {
@@ -1264,9 +1263,9 @@ __global__ void k_init_mosquitoes(Dev d)
             const float base = cdf_at(d.cdfm, d.am, a != 0 ? (int32_t)a - 1 : 0);
             const float ple = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, base), u01(r.v[2])), base);
             d.m_state[i] = 0;
-            d.m_age[i] = (int32_t)a;
+            d.m_born[i] = -(int32_t)a;
             d.m_ple[i] = ple;
-            d.m_dage[i] = death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f);
+            d.m_dtime[i] = death_time(-(int32_t)a, death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f));
         }
     }
     const uint32_t tile_dead = __reduce_add_sync(kFull, ndead);
@@ -1296,7 +1295,7 @@ __global__ void k_seed(Dev d)
         const uint32_t rr = (uint32_t)resolve(d.recovery, r.v[2]);
         const uint32_t m = rr > 1u ? rr - 1u : 1u;
         const int32_t dur = (int32_t)(bounded(r.v[1], m) + 1u);
-        d.n_recovery[i] = (d.quirks & ARBO_QUIRK_SEED_RECOVERY_DURATION) ? dur : d.n_age[i] + dur;
+        d.n_recovery[i] = (d.quirks & ARBO_QUIRK_SEED_RECOVERY_DURATION) ? dur : dur - d.n_born[i];  // age + dur
         atomicAdd(&d.infh[s * d.P + comm_of(d.nloc, d.P, i)], 1u);
     }
     if (j < d.mInit) {

@@ -1,11 +1,11 @@
 // sim_internal.h — device-side layout of one simulation and the kernel launchers.
 //
 // Layout in HBM (structure of arrays, every array 256-byte aligned, one allocation):
-//   humans   (N padded to a multiple of 4 agents):  age i32, death_age i32, status u8,
-//            exposed i32, recovery i32, ple f32, strain u8, immunity u8.
-//   mosquito (M padded to whole 128-slot tiles):     age i32, death_age i32, state u8
+//   humans   (N padded to a multiple of 4 agents):  birth time i32, death time i32,
+//            status u8, exposed i32, recovery i32, ple f32, strain u8, immunity u8.
+//   mosquito (M padded to whole 128-slot tiles):     birth time i32, death time i32, state u8
 //            (bits 0-1 status, bit 7 dead), exposed i32, ple f32, strain u8; tile dead
-//            count i32 per tile.
+//            count i32 per tile. Exposed and recovery hold ages, as in the reference.
 //   The census is community-sorted: community c owns the contiguous index range
 //   [loc[c], loc[c+1]) of each species, so infection draws hit contiguous ranges and a
 //   128-slot tile spans one or two communities.
@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
 #include <string>
 
 #include "philox.cuh"
@@ -29,6 +30,12 @@ namespace arbo {
 constexpr uint8_t kPad = 0xFF;        // status byte of a padding agent
 constexpr uint8_t kDead = 0x80;       // mosquito state: dead flag
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// Death time of an agent born at time `born` with death age `dage` (INT_MAX: never dies).
+__host__ __device__ inline int32_t death_time(int32_t born, int32_t dage)
+{
+    return dage == INT_MAX ? INT_MAX : born + dage;
+}
 
 constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
@@ -52,18 +59,23 @@ struct Dev {
     // parameters
     float biting, mnSuccess, nmSuccess, recovery, mExposed, nExposed, extInf, longDist, noDist, seroPrev;
     uint32_t maxIntro, maxTarget, quirks, recordSpatial, nInit, mInit;
+    // Ages are kept as birth and death times, so that the demographic pass reads the status
+    // byte and the death time of an agent and writes nothing for a survivor without a
+    // transition: age at time t = t - born; the agent dies in the step that reaches time
+    // t >= dtime (its age then reaches its death age; INT_MAX: never).
     // humans
-    int32_t* n_age;
-    int32_t* n_dage;
+    int32_t* n_born;
+    int32_t* n_dtime;
     uint8_t* n_status;
     int32_t* n_exposed;
     int32_t* n_recovery;
     float* n_ple;
     uint8_t* n_strain;
     uint8_t* n_imm;
-    // mosquitoes
-    int32_t* m_age;
-    int32_t* m_dage;
+    // mosquitoes (a dead slot keeps the times of its last life; a slot dead since
+    // initialisation has dtime == INT_MIN)
+    int32_t* m_born;
+    int32_t* m_dtime;
     uint8_t* m_state;
     int32_t* m_exposed;
     float* m_ple;

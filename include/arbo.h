@@ -297,7 +297,10 @@ int arbo_sim_get_series(arbo_sim* s, arbo_series_kind kind, uint32_t* host, size
 int arbo_sim_get_counters(arbo_sim* s, arbo_counter_kind kind, void* host, size_t n, void* stream);
 
 /* Copy / overwrite a census field (bytes = element count * element size). Setting a field
- * does not update the counters; arbo_sim_set_counters does. Test and resume hooks. */
+ * does not update the counters; arbo_sim_set_counters does. Test and resume hooks. The
+ * device keeps birth and death times instead of ages, so the age and death-age fields are
+ * computed on the copy (at the current step; a dead mosquito slot reads the age at which it
+ * died) and cannot be set (ARBO_ERR_INVALID). */
 int arbo_sim_get_census(arbo_sim* s, arbo_census_field field, void* host, size_t bytes, void* stream);
 int arbo_sim_set_census(arbo_sim* s, arbo_census_field field, const void* host, size_t bytes, void* stream);
 int arbo_sim_set_counters(arbo_sim* s, arbo_counter_kind kind, const void* host, size_t n, void* stream);
