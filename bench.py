@@ -32,19 +32,22 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# Algorithmic bytes of the demographic pass: every agent's status byte and death time are read
-# (ages are kept as birth times, so a survivor writes nothing); each birth writes the newborn's
-# PLE, birth time and death time (12) and a status byte, plus the status byte of the death that
-# freed its slot (a human's death and rebirth are one event: status and immunity bytes).
-BYTES_PER_AGENT_STEP = 5
-BYTES_PER_BIRTH = 14
+# Algorithmic bytes per agent-step of the demographic pass, the roofline figure: what the
+# reference's algorithm moves per agent (read age 4 + death age 4 + status 1, write age 4).
+BYTES_PER_AGENT_STEP = 13
+# What this library's layout moves instead: ages are kept as birth times, so every agent costs
+# its status byte and death time (5) and a survivor writes nothing; each birth writes the
+# newborn's PLE, birth time and death time (12) and a status byte, plus the status byte of the
+# death that freed its slot (a human's death and rebirth are one event: status and immunity).
+LAYOUT_BYTES_PER_AGENT_STEP = 5
+LAYOUT_BYTES_PER_BIRTH = 14
 FLUSH_MB = 320
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # Per-launch DRAM traffic of the demographic kernel on this workload, from the ncu capture
-# summarised in profiles/k_demog_plain_large.md (dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch); None until captured for the current kernel.
-DEMOG_TRAFFIC_BYTES = None
+# summarised in profiles/k_demog_plain_large.md: dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch (44,204,032 + 8,091,392 bytes).
+DEMOG_TRAFFIC_BYTES = 52_295_424
 
 
 def parse():
@@ -305,8 +308,9 @@ def ours_arm(args, world, rank, local):
     sim.close()
     demog_ms = phases[0]
     peak, peak_kind = hbm_peak()
-    demog_bytes = BYTES_PER_AGENT_STEP * w.agents + BYTES_PER_BIRTH * births
-    achieved = demog_bytes / (demog_ms * 1e-3) / 1e9
+    achieved = BYTES_PER_AGENT_STEP * w.agents / (demog_ms * 1e-3) / 1e9
+    layout_bytes = LAYOUT_BYTES_PER_AGENT_STEP * w.agents + LAYOUT_BYTES_PER_BIRTH * births
+    layout_gbs = layout_bytes / (demog_ms * 1e-3) / 1e9
     traffic = DEMOG_TRAFFIC_BYTES * (w.agents / 7_000_000) if DEMOG_TRAFFIC_BYTES else None
 
     # --- end to end: the reference-facing call with host buffers (create + upload, init, a full
@@ -335,8 +339,10 @@ def ours_arm(args, world, rank, local):
         "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": config_block(w, args, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_demog", "peak_kind": peak_kind,
-                     "bytes_per_agent_step": BYTES_PER_AGENT_STEP, "bytes_per_birth": BYTES_PER_BIRTH,
-                     "births_per_step": births, "algorithmic_bytes": demog_bytes, "kernel_ms": demog_ms,
+                     "bytes_per_agent_step": BYTES_PER_AGENT_STEP, "kernel_ms": demog_ms,
+                     "layout": {"bytes": layout_bytes, "bytes_per_agent_step": LAYOUT_BYTES_PER_AGENT_STEP,
+                                "bytes_per_birth": LAYOUT_BYTES_PER_BIRTH, "births_per_step": births,
+                                "achieved": layout_gbs, "frac": layout_gbs / peak},
                      "phase_ms": {"demographic": phases[0], "foi_series": phases[1], "infection": phases[2],
                                   "step": phases[3]}},
         "e2e": {"value": e2e_value, "unit": "agent-steps/s", "h2d_bytes_per_step": io[0] / 3650,
@@ -393,7 +399,6 @@ def batched_measure(args, seed):
         "instances": len(ws), "agents": agents, "steps": K,
         "value": agents * K / batched_s, "unit": "agent-steps/s", "ms_per_step": batched_s * 1e3 / K,
         "sequential_value": agents * K / (seq_ms / 1e3), "speedup_vs_sequential": (seq_ms / 1e3) / batched_s,
-        # whole batch step against the demographic pass's per-agent floor (births not counted)
         "roofline_frac_step": BYTES_PER_AGENT_STEP * agents * K / batched_s / 1e9 / hbm_peak()[0],
         "phase_ms": {"demographic": phases[0], "foi_series": phases[1], "infection": phases[2], "step": phases[3]},
         "autotuned": {"demogBlock": arch.demogBlock, "demogUnroll": arch.demogUnroll, "foiBlock": arch.foiBlock,
