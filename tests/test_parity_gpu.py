@@ -163,3 +163,24 @@ def test_invariants_large_shape(gpu):
         assert np.array_equal(mcnt, sim.counters("m_subpop_count"))
         assert sim.status()[0] == 0
     assert np.all(sim.series("n_count") == 100_000)
+
+
+def test_census_ages_derived_and_read_only(gpu):
+    # Ages are kept as birth and death times on the device: the census reads them back as the
+    # reference's fields (checked against the oracle above) and refuses to set them; the other
+    # fields round-trip.
+    from arbo_gpu_fit_gb300 import _native
+
+    w = small_case(seed=9, T=12, mosBaseRatio=0.5)  # about half the slots dead
+    sim, orc = pair(w)
+    run_and_compare(sim, orc, [5])
+    for f in ("n_age", "n_death_age", "m_age", "m_death_age"):
+        with pytest.raises(_native.ArboError):
+            sim.set_census(f, sim.census(f))
+    ple = sim.census("m_ple")
+    sim.set_census("m_ple", ple)
+    assert np.array_equal(sim.census("m_ple"), ple)
+    # Dead slots read the age at which they died (0 for slots dead since initialisation).
+    dead = sim.census("m_dead") == 1
+    assert dead.any() and np.all(sim.census("m_age")[dead] >= 0)
+    compare_state(sim, orc, "after set_census")
