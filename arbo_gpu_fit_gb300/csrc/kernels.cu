@@ -788,13 +788,16 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
 
 // ------------------------------------------------------------------ infection draws
 
-// Infection of human i in step t, after the demographic pass of the step: its age is t + 1 - born.
-__device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r, uint32_t t)
+// Infection of human i in step t, after the demographic pass of the step. `imm` and `born` are
+// its immunity byte and birth time, loaded by the caller together with the winner key (its age
+// is t + 1 - born).
+__device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r, uint32_t t,
+                                             uint32_t imm, int32_t born)
 {
     d.n_status[i] = 1;
     d.n_strain[i] = (uint8_t)s;
-    d.n_imm[i] = (uint8_t)(d.n_imm[i] | (1u << s));
-    const int32_t age = (int32_t)t + 1 - d.n_born[i];
+    d.n_imm[i] = (uint8_t)(imm | (1u << s));
+    const int32_t age = (int32_t)t + 1 - born;
     const int32_t ex = (int32_t)resolve(__fadd_rn((float)age, d.nExposed), r.v[0]);
     d.n_exposed[i] = ex;
     d.n_recovery[i] = (int32_t)resolve(__fadd_rn((float)ex, d.recovery), r.v[1]);
@@ -803,9 +806,9 @@ __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t 
 // Target of mosquito event e: the first alive slot of its attempt sequence (dead slots are
 // retried, cpp/mepidemic.cu:206-235). Returns UINT_MAX when the attempts run out. The four
 // candidates of one Philox call are loaded together (one memory round trip) and the first alive
-// one in attempt order is taken.
+// one in attempt order is taken; its state byte is left in *state.
 __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key, uint32_t pidx, uint32_t e,
-                                                    uint32_t base, uint32_t size, uint32_t t)
+                                                    uint32_t base, uint32_t size, uint32_t t, uint32_t* state)
 {
     for (uint32_t a = 0; a < d.maxTarget; a += 4) {
         const U4 r = draw4(key, kInfMTarget, pidx, t, e, a >> 2);
@@ -816,7 +819,10 @@ __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key
         for (int q = 0; q < 4; ++q) st[q] = (a + q < d.maxTarget) ? __ldcg(&d.m_state[slot[q]]) : (uint32_t)kDead;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            if (!(st[q] & kDead)) return slot[q];
+            if (!(st[q] & kDead)) {
+                *state = st[q];
+                return slot[q];
+            }
     }
     return UINT_MAX;
 }
@@ -981,10 +987,11 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
             }
         } else {
             const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
-            const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
+            uint32_t st = 0;
+            const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t, &st);
             if (it < kTargetCache) sh.target[it].x = slot;
             if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
-            else if (d.m_state[slot] == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
+            else if (st == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
         }
     }
     __syncthreads();
@@ -1001,12 +1008,13 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 bool elig = false;
                 uint32_t i = 0;
                 unsigned long long okey = 0;
+                uint32_t im = 0;
                 if (a < d.maxIntro) {
                     const U4 r = draw4(key, kIntroTarget, ph, t, a >> 2);
                     i = nbase + bounded(r.v[a & 3], ns);
                     okey = order_key(hiword, j, 1, a);
-                    elig = __ldcg(&d.n_status[i]) == 0 && !((__ldcg(&d.n_imm[i]) >> s) & 1u) &&
-                           __ldcg(&d.winh[i]) > okey;
+                    im = __ldcg(&d.n_imm[i]);
+                    elig = __ldcg(&d.n_status[i]) == 0 && !((im >> s) & 1u) && __ldcg(&d.winh[i]) > okey;
                 }
                 const unsigned bal = __ballot_sync(kFull, elig);
                 if (!bal) {
@@ -1016,7 +1024,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 const uint32_t pl = __ffs(bal) - 1;
                 if (lane == pl) {
                     d.winh[i] = okey;
-                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t);
+                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t, im, __ldcg(&d.n_born[i]));
                 }
                 __syncwarp();
                 left -= 1;
@@ -1046,22 +1054,45 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
 #pragma unroll
                 for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
             }
+            // Winner keys and the inputs of the infection in one round trip: only the winner of a
+            // target writes it, so the values read here are the ones the infection needs.
+            unsigned long long wk[4];
+            uint32_t im[4];
+            int32_t bn[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                wk[q] = 0;
+                im[q] = 0;
+                bn[q] = 0;
+                if (4 * idx + q < k) {
+                    wk[q] = __ldcg(&d.winh[tg[q]]);
+                    im[q] = __ldcg(&d.n_imm[tg[q]]);
+                    bn[q] = __ldcg(&d.n_born[tg[q]]);
+                }
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const uint32_t e = 4 * idx + q;
                 if (e >= k) break;
-                if (__ldcg(&d.winh[tg[q]]) == order_key(hiword, j, 0, e))
-                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t);
+                if (wk[q] == order_key(hiword, j, 0, e))
+                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t, im[q], bn[q]);
             }
         } else {
             const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+            uint32_t st = 0;
             const uint32_t slot = it < kTargetCache ? sh.target[it].x
-                                                    : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t);
-            if (slot != UINT_MAX && __ldcg(&d.winm[slot]) == order_key(hiword, j, 0, idx)) {
+                                                    : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t, &st);
+            unsigned long long wk = 0;
+            int32_t bn = 0;
+            if (slot != UINT_MAX) {  // winner key and birth time in one round trip
+                wk = __ldcg(&d.winm[slot]);
+                bn = __ldcg(&d.m_born[slot]);
+            }
+            if (slot != UINT_MAX && wk == order_key(hiword, j, 0, idx)) {
                 const U4 r = draw4(key, kInfMExposed, pm, t, idx >> 2);
                 d.m_state[slot] = 1;
                 d.m_strain[slot] = (uint8_t)sm;
-                const int32_t age = (int32_t)t + 1 - d.m_born[slot];
+                const int32_t age = (int32_t)t + 1 - bn;
                 d.m_exposed[slot] = (int32_t)resolve(__fadd_rn((float)age, d.mExposed), r.v[idx & 3]);
             }
         }
