@@ -207,7 +207,7 @@ int arbo_arch_param_query(arbo_arch_param* a, int device)
     a->demogBlock = 256;
     a->demogUnroll = 2;
     a->foiBlock = 256;
-    a->infectBlock = 128;  // two communities per CTA: fastest on the large workload (launch-shape sweep)
+    a->infectBlock = 64;  // two communities (one warp each) per CTA: fastest on the large workload
     a->graphSteps = 64;
     a->demogPipeline = 0;
     int n = 0;
@@ -1211,7 +1211,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     l.numSM = a.totalSM ? a.totalSM : 152u;
     l.pdl = 1;
     std::vector<uint32_t> demog_off(n + 1, 0), demog_h(n, 0), foi_off(n + 1, 0), infect_off(n + 1, 0);
-    const uint32_t K = a.infectBlock >= 64 ? a.infectBlock / 64 : 1u;
+    const uint32_t K = a.infectBlock / 32;
     for (uint32_t i = 0; i < n; ++i) {
         const Dev& d = b->sims[i]->d;
         const uint64_t hb = cdiv(d.nvec, (uint64_t)32 * a.demogUnroll);  // warp items

@@ -867,7 +867,9 @@ __device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, ui
     }
 }
 
-// Infection draws. A CTA of 64*K threads owns K communities. Warp w < K reads community w's
+// Infection draws. A CTA of 32*K threads owns K communities, one warp each (more threads per
+// community measured slower: the pass is a chain of dependent round trips per community, so the
+// more communities in flight per SM the better). Warp w reads community w's
 // event counts (lanes 0..S-1), draws its introduction counts and first serotypes in parallel
 // lanes, and posts the per-serotype tables; the events of the K communities (groups of four
 // human events, single mosquito events) then form one index space shared by all the CTA's threads:
@@ -879,7 +881,7 @@ __device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, ui
 //   C: each event that won its target applies its infection.
 // This reproduces the serial loops of nmTransmission / mnTransmission (cpp/mepidemic.cu:143-246,
 // cpp/nepidemic.cu:146-319): a target is infected by the first eligible event in serial order.
-// Communities cb..cb+K-1 of one simulation (K = blockDim.x / 64, at least 1).
+// Communities cb..cb+K-1 of one simulation (K = blockDim.x / 32).
 __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t koff, InfectSmem& sh)
 {
     const uint32_t t = d.ctrl->t + koff;
@@ -887,7 +889,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
     const uint32_t hiword = ~epoch;
     const Key key = load_key(d.ctrl);
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
+    const uint32_t K = blockDim.x >> 5;
     const uint32_t S = d.S, P = d.P;
     const float ext = __fdiv_rn(d.extInf, (float)P);
     const uint32_t c = cb + warp;
@@ -1103,7 +1105,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
 __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
 {
     __shared__ InfectSmem sh;
-    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
+    const uint32_t K = blockDim.x >> 5;
     for (uint32_t cb = blockIdx.x * K; cb < d.P; cb += gridDim.x * K) infect_block(d, cb, koff, sh);
 }
 
@@ -1200,7 +1202,7 @@ __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
 __global__ void __launch_bounds__(512) k_infect_batch(BatchDev bd, uint32_t koff)
 {
     __shared__ InfectSmem sh;
-    const uint32_t K = blockDim.x >= 64 ? (blockDim.x >> 6) : 1u;
+    const uint32_t K = blockDim.x >> 5;
     batch_loop(bd, bd.infect_off, [&](const Dev& d, uint32_t, uint32_t b) { infect_block(d, b * K, koff, sh); });
 }
 
@@ -1443,7 +1445,7 @@ int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only,
 
 int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 {
-    const uint32_t per = l.infectBlock >= 64 ? l.infectBlock / 64 : 1u;
+    const uint32_t per = l.infectBlock / 32;
     uint32_t blocks = cdiv(d.P, per);
     const uint32_t cap = 16u * (l.numSM ? l.numSM : 152u);
     if (blocks > cap) blocks = cap;
