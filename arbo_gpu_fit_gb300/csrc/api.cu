@@ -1211,13 +1211,13 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     l.numSM = a.totalSM ? a.totalSM : 152u;
     l.pdl = 1;
     std::vector<uint32_t> demog_off(n + 1, 0), demog_h(n, 0), foi_off(n + 1, 0), infect_off(n + 1, 0);
-    const uint32_t K = a.infectBlock / 32;
+    const uint32_t K = a.infectBlock / 32;  // communities (warps) per infection CTA
     for (uint32_t i = 0; i < n; ++i) {
         const Dev& d = b->sims[i]->d;
         const uint64_t hb = cdiv(d.nvec, (uint64_t)32 * a.demogUnroll);  // warp items
         const uint64_t mb = cdiv(d.tiles, kQuad);
         const uint64_t fb = cdiv((uint64_t)d.S * d.P, a.foiBlock / 4);
-        const uint64_t ib = cdiv(d.P, K);
+        const uint64_t ib = d.P;  // the infection kernel takes communities, one warp each
         if (demog_off[i] + hb + mb >= (1ull << 31) || foi_off[i] + fb >= (1ull << 31) ||
             infect_off[i] + ib >= (1ull << 31))
             return fail(ARBO_ERR_INVALID, "batch too large: more than 2^31 blocks in one phase");
@@ -1260,7 +1260,11 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     b->blocks[2] = infect_off[n];
     bd.grid_demog = std::max(1u, std::min(b->blocks[0], l.numSM * occ[0]));
     bd.grid_foi = std::max(1u, std::min(b->blocks[1], l.numSM * occ[1]));
-    bd.grid_infect = std::max(1u, std::min(b->blocks[2], l.numSM * occ[2]));
+    // Runs of consecutive communities per warp (fewer descriptor restagings), as long as every
+    // resident warp still gets one.
+    const uint32_t warps = l.numSM * occ[2] * K;
+    bd.infect_run = std::max(1u, std::min(kInfectRunMax, b->blocks[2] / std::max(warps, 1u)));
+    bd.grid_infect = std::max(1u, std::min(cdiv(cdiv(b->blocks[2], bd.infect_run), K), l.numSM * occ[2]));
     batch_drop_graphs(b);
     b->bd = bd;
     b->l = l;

@@ -827,158 +827,107 @@ __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key
     return UINT_MAX;
 }
 
-// Per-CTA tables of the infection kernel: the CTA's K communities (one per warp) and their
-// events of every serotype flattened into one index space.
-constexpr uint32_t kTargetCache = 1024;  // items whose targets Phase A keeps for Phase C
+// Per-warp tables of the infection pass: one community and its events of every serotype
+// flattened into one index space.
+constexpr uint32_t kTargetCache = 128;  // items whose targets Phase A keeps for Phase C
 
-struct InfectSmem {
-    uint4 target[kTargetCache];          // per item: four human targets, or a mosquito slot in .x
-    uint32_t cstart[17];                 // flattened item start of each community (K+1)
-    uint32_t hstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, human groups
-    uint32_t mstart[16][ARBO_MAX_STRAINS]; // first item of serotype position j, mosquito events
-    uint32_t kh[16][ARBO_MAX_STRAINS];     // human events by position
-    uint32_t km[16][ARBO_MAX_STRAINS];     // mosquito events by position
-    uint32_t hitems[16];                 // human groups of the community
-    uint32_t c[16], s0h[16], s0m[16], nbase[16], mbase[16], ns[16], ms[16];
+struct InfectWarpSmem {
+    uint4 target[kTargetCache];         // per item: four human targets, or a mosquito slot in .x
+    uint32_t hstart[ARBO_MAX_STRAINS];  // first item of serotype position j, human groups
+    uint32_t mstart[ARBO_MAX_STRAINS];  // first item of serotype position j, mosquito events
+    uint32_t kh[ARBO_MAX_STRAINS];      // human events by position
+    uint32_t km[ARBO_MAX_STRAINS];      // mosquito events by position
 };
 
-// Decodes flattened item `it` of the CTA: community slot w, serotype position j, and either a
-// human group r4 (human == true) or a mosquito event e.
-__device__ __forceinline__ void decode_item(const InfectSmem& sh, uint32_t K, uint32_t S, uint32_t it, uint32_t* w,
-                                            uint32_t* j, bool* human, uint32_t* idx)
+// Serotype position of item `rel` of a table of starts (the last position whose start is <= rel;
+// positions without items share the next one's start).
+__device__ __forceinline__ uint32_t item_position(const uint32_t* start, uint32_t S, uint32_t rel)
 {
-    uint32_t ww = 0;
-    while (ww + 1 < K && sh.cstart[ww + 1] <= it) ++ww;
-    uint32_t rel = it - sh.cstart[ww];
-    *w = ww;
-    if (rel < sh.hitems[ww]) {
-        uint32_t jj = 0;
-        while (jj + 1 < S && sh.hstart[ww][jj + 1] <= rel) ++jj;
-        *j = jj;
-        *human = true;
-        *idx = rel - sh.hstart[ww][jj];
-    } else {
-        rel -= sh.hitems[ww];
-        uint32_t jj = 0;
-        while (jj + 1 < S && sh.mstart[ww][jj + 1] <= rel) ++jj;
-        *j = jj;
-        *human = false;
-        *idx = rel - sh.mstart[ww][jj];
-    }
+    uint32_t j = 0;
+    while (j + 1 < S && start[j + 1] <= rel) ++j;
+    return j;
 }
 
-// Infection draws. A CTA of 32*K threads owns K communities, one warp each (more threads per
-// community measured slower: the pass is a chain of dependent round trips per community, so the
-// more communities in flight per SM the better). Warp w reads community w's
-// event counts (lanes 0..S-1), draws its introduction counts and first serotypes in parallel
-// lanes, and posts the per-serotype tables; the events of the K communities (groups of four
-// human events, single mosquito events) then form one index space shared by all the CTA's threads:
+// Infection draws of community c, by one warp. Lanes 0..S-1 read the community's event counts
+// and draw its introduction counts, lanes 8 and 9 the first serotypes; the events (groups of
+// four human events, single mosquito events) then form one index space walked by the 32 lanes:
 //   A: every event whose target is eligible at the start of the pass bids its serial order
 //      (serotype position j, event index) for the target with atomicMin; the targets of the first
 //      kTargetCache items are kept in shared memory for phase C;
-//   B: external introductions (cpp/nepidemic.cu:261-309), per community in serial order, one warp
-//      testing 32 attempts at a time;
+//   B: external introductions (cpp/nepidemic.cu:261-309) in serial order, 32 attempts at a time;
 //   C: each event that won its target applies its infection.
 // This reproduces the serial loops of nmTransmission / mnTransmission (cpp/mepidemic.cu:143-246,
 // cpp/nepidemic.cu:146-319): a target is infected by the first eligible event in serial order.
-// Communities cb..cb+K-1 of one simulation (K = blockDim.x / 32).
-__device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t koff, InfectSmem& sh)
+// Every target of community c's events and introductions lies in c's own census range, so no
+// other warp reads or writes them during the pass and warp barriers order the phases. One warp
+// per community with no block barrier: the pass is a chain of dependent round trips per
+// community, so the more communities in flight per SM the better.
+__device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t koff, InfectWarpSmem& sh)
 {
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t t = d.ctrl->t + koff;
-    const uint32_t epoch = d.ctrl->epoch + koff;
-    const uint32_t hiword = ~epoch;
+    const uint32_t hiword = ~(d.ctrl->epoch + koff);
     const Key key = load_key(d.ctrl);
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = blockDim.x >> 5;
     const uint32_t S = d.S, P = d.P;
     const float ext = __fdiv_rn(d.extInf, (float)P);
-    const uint32_t c = cb + warp;
-    const bool owner = warp < K && c < P;
-    uint32_t ne = 0;
-    uint32_t items = 0;
-    if (owner) {
-        // Static loads and keyed draws first; the event counts and alive mosquitoes written by
-        // the previous kernels are read after the programmatic-launch wait.
-        const uint32_t ns = __ldg(&d.nsize[c]);
-        const uint32_t ms = __ldg(&d.msize[c]);
-        const uint32_t nb0 = __ldg(&d.nloc[c]), mb0 = __ldg(&d.mloc[c]);
-        const uint32_t pl = lane * P + c;
-        U4 rd;
-        if (lane < S) rd = draw4(key, kIntroCount, pl, t);
-        else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
-        else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
-        griddep_wait();
-        const uint32_t mc = d.mcnt[c];
-        uint32_t kh = lane < S ? d.transh[pl] : 0u;
-        uint32_t km = lane < S ? d.transm[pl] : 0u;
-        uint32_t sv = 0;
-        if (lane < S) {
-            if (kh) d.transh[pl] = 0;
-            if (km) d.transm[pl] = 0;
-            if (ns == 0) kh = 0;
-            else ne = (uint32_t)resolve(ext, rd.v[0]);
-            if (mc == 0) km = 0;
-            if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
-                atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
-                kh = min(kh, kMaxEventsPerPair - 1);
-                km = min(km, kMaxEventsPerPair - 1);
-            }
-        } else if (lane == 8) {
-            if (mc) sv = bounded(rd.v[0], S);
-        } else if (lane == 9) {
-            if (ns) sv = bounded(rd.v[0], S);
-        }
-        const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
-        uint32_t H = 0, Mt = 0;
-        for (uint32_t j = 0; j < S; ++j) {
-            const uint32_t khj = __shfl_sync(kFull, kh, (s0h + j) % S);
-            const uint32_t kmj = __shfl_sync(kFull, km, (s0m + j) % S);
-            if (lane == 0) {
-                sh.hstart[warp][j] = H;
-                sh.mstart[warp][j] = Mt;
-                sh.kh[warp][j] = khj;
-                sh.km[warp][j] = kmj;
-            }
-            H += (khj + 3) >> 2;
-            Mt += kmj;
-        }
-        if (lane == 0) {
-            sh.hitems[warp] = H;
-            sh.c[warp] = c;
-            sh.s0h[warp] = s0h;
-            sh.s0m[warp] = s0m;
-            sh.nbase[warp] = nb0;
-            sh.mbase[warp] = mb0;
-            sh.ns[warp] = ns;
-            sh.ms[warp] = ms;
-        }
-        items = H + Mt;
-    }
+    // Static loads and keyed draws first; the event counts and alive mosquitoes written by the
+    // previous kernels are read after the programmatic-launch wait.
+    const uint32_t ns = __ldg(&d.nsize[c]), ms = __ldg(&d.msize[c]);
+    const uint32_t nbase = __ldg(&d.nloc[c]), mbase = __ldg(&d.mloc[c]);
+    const uint32_t pl = lane * P + c;
+    U4 rd;
+    if (lane < S) rd = draw4(key, kIntroCount, pl, t);
+    else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
+    else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
     griddep_wait();
-    // Item starts of the K communities (serial over at most 8 entries).
-    if (lane == 0 && warp < K) sh.cstart[warp + 1] = items;
-    __syncthreads();
-    if (tid == 0) {
-        sh.cstart[0] = 0;
-        for (uint32_t w = 1; w <= K; ++w) sh.cstart[w] += sh.cstart[w - 1];
+    const uint32_t mc = d.mcnt[c];
+    uint32_t kh = lane < S ? d.transh[pl] : 0u;
+    uint32_t km = lane < S ? d.transm[pl] : 0u;
+    uint32_t sv = 0, ne = 0;
+    if (lane < S) {
+        if (kh) d.transh[pl] = 0;
+        if (km) d.transm[pl] = 0;
+        if (ns == 0) kh = 0;
+        else ne = (uint32_t)resolve(ext, rd.v[0]);
+        if (mc == 0) km = 0;
+        if (kh >= kMaxEventsPerPair || km >= kMaxEventsPerPair) {
+            atomicOr(&d.ctrl->err, ARBO_DEVERR_EVENT_OVERFLOW);
+            kh = min(kh, kMaxEventsPerPair - 1);
+            km = min(km, kMaxEventsPerPair - 1);
+        }
+    } else if (lane == 8) {
+        if (mc) sv = bounded(rd.v[0], S);
+    } else if (lane == 9) {
+        if (ns) sv = bounded(rd.v[0], S);
     }
-    __syncthreads();
-    const uint32_t total = sh.cstart[K];
-    const uint32_t any_intro = __syncthreads_or(ne != 0);
-    if (total == 0 && !any_intro) return;
+    const uint32_t s0m = __shfl_sync(kFull, sv, 8), s0h = __shfl_sync(kFull, sv, 9);
+    uint32_t H = 0, Mt = 0;
+    for (uint32_t j = 0; j < S; ++j) {
+        const uint32_t khj = __shfl_sync(kFull, kh, (s0h + j) % S);
+        const uint32_t kmj = __shfl_sync(kFull, km, (s0m + j) % S);
+        if (lane == 0) {
+            sh.hstart[j] = H;
+            sh.mstart[j] = Mt;
+            sh.kh[j] = khj;
+            sh.km[j] = kmj;
+        }
+        H += (khj + 3) >> 2;
+        Mt += kmj;
+    }
+    __syncwarp();
+    const uint32_t items = H + Mt;
+    const bool any_intro = __any_sync(kFull, ne != 0);
+    if (items == 0 && !any_intro) return;
 
     // Phase A
-    for (uint32_t it = tid; it < total; it += blockDim.x) {
-        uint32_t w, j, idx;
-        bool human;
-        decode_item(sh, K, S, it, &w, &j, &human, &idx);
-        const uint32_t cc = sh.c[w];
-        if (human) {
-            const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+    for (uint32_t it = lane; it < items; it += 32) {
+        if (it < H) {
+            const uint32_t j = item_position(sh.hstart, S, it), idx = it - sh.hstart[j];
+            const uint32_t s = (s0h + j) % S, ph = s * P + c, k = sh.kh[j];
             const U4 r = draw4(key, kInfHTarget, ph, t, idx);
             uint32_t tg[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+            for (int q = 0; q < 4; ++q) tg[q] = nbase + bounded(r.v[q], ns);
             if (it < kTargetCache) sh.target[it] = make_uint4(tg[0], tg[1], tg[2], tg[3]);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -988,18 +937,18 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                 if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[tg[q]], order_key(hiword, j, 0, e));
             }
         } else {
-            const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+            const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
+            const uint32_t sm = (s0m + j) % S, pm = sm * P + c;
             uint32_t st = 0;
-            const uint32_t slot = mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t, &st);
+            const uint32_t slot = mosquito_target(d, key, pm, idx, mbase, ms, t, &st);
             if (it < kTargetCache) sh.target[it].x = slot;
             if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
             else if (st == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
         }
     }
-    __syncthreads();
-    // Phase B: warp w handles the introductions of its own community.
-    if (any_intro && owner) {
-        const uint32_t s0h = sh.s0h[warp], nbase = sh.nbase[warp], ns = sh.ns[warp];
+    __syncwarp();
+    // Phase B
+    if (any_intro) {
         for (uint32_t j = 0; j < S; ++j) {
             const uint32_t s = (s0h + j) % S, ph = s * P + c;
             uint32_t left = __shfl_sync(kFull, ne, s);
@@ -1023,27 +972,24 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                     a0 += 32;
                     continue;
                 }
-                const uint32_t pl = __ffs(bal) - 1;
-                if (lane == pl) {
+                const uint32_t pl2 = __ffs(bal) - 1;
+                if (lane == pl2) {
                     d.winh[i] = okey;
                     infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t, im, __ldcg(&d.n_born[i]));
                 }
                 __syncwarp();
                 left -= 1;
-                a0 = a0 + pl + 1;
+                a0 = a0 + pl2 + 1;
             }
             if (left > 0 && lane == 0) atomicAdd(&d.ctrl->diag[1], 1u);
         }
+        __syncwarp();
     }
-    __syncthreads();
     // Phase C
-    for (uint32_t it = tid; it < total; it += blockDim.x) {
-        uint32_t w, j, idx;
-        bool human;
-        decode_item(sh, K, S, it, &w, &j, &human, &idx);
-        const uint32_t cc = sh.c[w];
-        if (human) {
-            const uint32_t s = (sh.s0h[w] + j) % S, ph = s * P + cc, k = sh.kh[w][j];
+    for (uint32_t it = lane; it < items; it += 32) {
+        if (it < H) {
+            const uint32_t j = item_position(sh.hstart, S, it), idx = it - sh.hstart[j];
+            const uint32_t s = (s0h + j) % S, ph = s * P + c, k = sh.kh[j];
             uint32_t tg[4];
             if (it < kTargetCache) {
                 const uint4 v = sh.target[it];
@@ -1054,7 +1000,7 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
             } else {
                 const U4 r = draw4(key, kInfHTarget, ph, t, idx);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) tg[q] = sh.nbase[w] + bounded(r.v[q], sh.ns[w]);
+                for (int q = 0; q < 4; ++q) tg[q] = nbase + bounded(r.v[q], ns);
             }
             // Winner keys and the inputs of the infection in one round trip: only the winner of a
             // target writes it, so the values read here are the ones the infection needs.
@@ -1080,10 +1026,10 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
                     infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t, im[q], bn[q]);
             }
         } else {
-            const uint32_t sm = (sh.s0m[w] + j) % S, pm = sm * P + cc;
+            const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
+            const uint32_t sm = (s0m + j) % S, pm = sm * P + c;
             uint32_t st = 0;
-            const uint32_t slot = it < kTargetCache ? sh.target[it].x
-                                                    : mosquito_target(d, key, pm, idx, sh.mbase[w], sh.ms[w], t, &st);
+            const uint32_t slot = it < kTargetCache ? sh.target[it].x : mosquito_target(d, key, pm, idx, mbase, ms, t, &st);
             unsigned long long wk = 0;
             int32_t bn = 0;
             if (slot != UINT_MAX) {  // winner key and birth time in one round trip
@@ -1099,14 +1045,17 @@ __device__ __forceinline__ void infect_block(const Dev& d, uint32_t cb, uint32_t
             }
         }
     }
-    __syncthreads();
+    __syncwarp();  // the warp's tables are reused for its next community
 }
 
+// One warp per community: warp w of block b takes communities b*K + w, + gridDim.x*K, ...
+// (K = blockDim.x / 32; K per-warp tables in dynamic shared memory).
 __global__ void __launch_bounds__(512) k_infect(Dev d, uint32_t koff)
 {
-    __shared__ InfectSmem sh;
-    const uint32_t K = blockDim.x >> 5;
-    for (uint32_t cb = blockIdx.x * K; cb < d.P; cb += gridDim.x * K) infect_block(d, cb, koff, sh);
+    extern __shared__ __align__(16) unsigned char infect_dyn[];
+    const uint32_t warp = threadIdx.x >> 5, K = blockDim.x >> 5;
+    InfectWarpSmem& sh = reinterpret_cast<InfectWarpSmem*>(infect_dyn)[warp];
+    for (uint32_t c = blockIdx.x * K + warp; c < d.P; c += gridDim.x * K) infect_warp(d, c, koff, sh);
 }
 
 // ------------------------------------------------------------------ batched steps
@@ -1199,11 +1148,47 @@ __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
     batch_loop(bd, bd.foi_off, [&](const Dev& d, uint32_t, uint32_t b) { foi_block(d, b, 0, koff, fs); });
 }
 
+// Infection pass of a batch: one warp per community over the concatenated communities of all
+// instances (bd.infect_off counts communities). Warps take runs of bd.infect_run consecutive
+// communities, strided over the grid, so that a warp restages its instance descriptor (per-warp
+// copy in shared memory, after its tables) about once per run while every instance is spread over
+// many warps.
 __global__ void __launch_bounds__(512) k_infect_batch(BatchDev bd, uint32_t koff)
 {
-    __shared__ InfectSmem sh;
-    const uint32_t K = blockDim.x >> 5;
-    batch_loop(bd, bd.infect_off, [&](const Dev& d, uint32_t, uint32_t b) { infect_block(d, b * K, koff, sh); });
+    extern __shared__ __align__(16) unsigned char infect_dyn[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, K = blockDim.x >> 5;
+    InfectWarpSmem& sh = reinterpret_cast<InfectWarpSmem*>(infect_dyn)[warp];
+    unsigned long long* wdev =
+        reinterpret_cast<unsigned long long*>(infect_dyn + K * sizeof(InfectWarpSmem)) + warp * (sizeof(Dev) / 8);
+    const Dev& d = *reinterpret_cast<const Dev*>(wdev);
+    const uint32_t total = __ldg(&bd.infect_off[bd.n]);
+    const uint32_t run = bd.infect_run, runs = (total + run - 1) / run;
+    const uint32_t gw = blockIdx.x * K + warp, nw = gridDim.x * K;
+    uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its community range
+    for (uint32_t r = gw; r < runs; r += nw) {
+        const uint32_t end = min(total, (r + 1) * run);
+        for (uint32_t it = r * run; it < end; ++it) {
+            if (inst == UINT_MAX || it < lo || it >= hi) {
+                inst = batch_instance(bd.infect_off, bd.n, it);
+                lo = __ldg(&bd.infect_off[inst]);
+                hi = __ldg(&bd.infect_off[inst + 1]);
+                __syncwarp();  // every lane is done with the previous descriptor
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
+                for (uint32_t i = lane; i < sizeof(Dev) / 8; i += 32) wdev[i] = src[i];
+                __syncwarp();
+            }
+            infect_warp(d, it - lo, koff, sh);
+        }
+    }
+}
+
+static_assert(16 * (sizeof(InfectWarpSmem) + sizeof(Dev)) <= 48 * 1024,
+              "per-warp infection tables of a 512-thread block must fit the default dynamic shared memory");
+
+// Dynamic shared memory of the infection kernels for blocks of `threads` threads.
+size_t infect_smem(uint32_t threads, bool batch)
+{
+    return (size_t)(threads / 32) * (sizeof(InfectWarpSmem) + (batch ? sizeof(Dev) : 0));
 }
 
 __global__ void k_advance_batch(BatchDev bd, uint32_t n)
@@ -1421,12 +1406,13 @@ int launch_demog(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
 // Launch with programmatic stream serialization: the kernel may start while the previous kernel
 // of the stream finishes; it calls griddepcontrol.wait before reading that kernel's results.
 template <typename... Args>
-static int launch_pdl(void (*kernel)(Args...), dim3 grid, dim3 block, cudaStream_t st, bool pdl, Args... args)
+static int launch_pdl(void (*kernel)(Args...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                      Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1440,7 +1426,7 @@ int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only,
 {
     const uint32_t SP = d.S * d.P;
     const uint32_t K = l.foiBlock / 4;
-    return launch_pdl(k_foi, dim3(cdiv(SP, K)), dim3(l.foiBlock), st, l.pdl && !collect_only, d, collect_only, koff);
+    return launch_pdl(k_foi, dim3(cdiv(SP, K)), dim3(l.foiBlock), 0, st, l.pdl && !collect_only, d, collect_only, koff);
 }
 
 int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
@@ -1449,7 +1435,8 @@ int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
     uint32_t blocks = cdiv(d.P, per);
     const uint32_t cap = 16u * (l.numSM ? l.numSM : 152u);
     if (blocks > cap) blocks = cap;
-    return launch_pdl(k_infect, dim3(blocks), dim3(l.infectBlock), st, l.pdl != 0, d, koff);
+    return launch_pdl(k_infect, dim3(blocks), dim3(l.infectBlock), infect_smem(l.infectBlock, false), st, l.pdl != 0, d,
+                      koff);
 }
 
 int launch_init(const Dev& d, const Launch& l, void* stream)
@@ -1498,7 +1485,8 @@ int batch_blocks_per_sm(const Launch& l, uint32_t out[3])
     out[0] = n > 0 ? (uint32_t)n : 1u;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_foi_batch, (int)l.foiBlock, 0)) != cudaSuccess) return (int)e;
     out[1] = n > 0 ? (uint32_t)n : 1u;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_infect_batch, (int)l.infectBlock, 0)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_infect_batch, (int)l.infectBlock,
+                                                            infect_smem(l.infectBlock, true))) != cudaSuccess)
         return (int)e;
     out[2] = n > 0 ? (uint32_t)n : 1u;
     return 0;
@@ -1516,9 +1504,10 @@ int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* e
     else k_demog_batch<1><<<gd, bdm, 0, st>>>(bd, koff);
     if ((e = (int)cudaGetLastError())) return e;
     if (ev) cudaEventRecord(ev[1], st);
-    if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), st, l.pdl != 0, bd, koff))) return e;
+    if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), 0, st, l.pdl != 0, bd, koff))) return e;
     if (ev) cudaEventRecord(ev[2], st);
-    if ((e = launch_pdl(k_infect_batch, dim3(bd.grid_infect), dim3(l.infectBlock), st, l.pdl != 0, bd, koff)))
+    if ((e = launch_pdl(k_infect_batch, dim3(bd.grid_infect), dim3(l.infectBlock), infect_smem(l.infectBlock, true), st,
+                        l.pdl != 0, bd, koff)))
         return e;
     if (ev) cudaEventRecord(ev[3], st);
     return 0;

@@ -40,6 +40,7 @@ __host__ __device__ inline int32_t death_time(int32_t born, int32_t dage)
 constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
 constexpr uint32_t kMaxEventsPerPair = 1u << 24;
+constexpr uint32_t kInfectRunMax = 4;  // most consecutive communities a warp of the batched infection kernel takes
 
 struct Ctrl {
     uint32_t t;          // current step
@@ -130,9 +131,10 @@ struct BatchDev {
     const uint32_t* demog_h;     // [n] human warp items of each instance (the rest are quads)
     uint32_t* work;              // demographic item counter (zero between steps)
     const uint32_t* foi_off;     // [n+1] force-of-infection blocks
-    const uint32_t* infect_off;  // [n+1] infection blocks (K communities each)
+    const uint32_t* infect_off;  // [n+1] communities (the infection kernel runs one warp per community)
     uint32_t n;
     uint32_t grid_demog, grid_foi, grid_infect;  // resident CTAs of each persistent kernel
+    uint32_t infect_run;                         // consecutive communities per warp run (1..kInfectRunMax)
 };
 
 struct Launch {
