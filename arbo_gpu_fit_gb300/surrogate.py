@@ -17,7 +17,7 @@ import numpy as np
 
 from . import configs
 from ._native import check, load
-from .mcmc import month_rows, monthly, sim_seed
+from .mcmc import chain_batch, month_rows, monthly, sim_seed
 
 _F = POINTER(c_float)
 
@@ -162,7 +162,7 @@ def training_set(workload: configs.Workload, n: int, months: int, seed: int = 0,
                  box=None, on_batch=None):
     """n parameter vectors uniform in the prior box and the simulator's monthly incidence for each,
     simulated in batches of batch_size instances (arbo_batch_*)."""
-    from .simulation import Batch, Parameter, Simulation
+    from .simulation import Simulation
 
     box = box if box is not None else configs.PRIOR_BOX
     lo = np.array([b[1] for b in box])
@@ -175,7 +175,7 @@ def training_set(workload: configs.Workload, n: int, months: int, seed: int = 0,
             for _ in range(min(batch_size, n))]
     inc = np.zeros((n, months, int(w.parameter.simulation.nStrains)), np.int64)
     try:
-        with Batch(sims) as b:
+        with chain_batch(sims) as b:
             for i0 in range(0, n, len(sims)):
                 k = min(len(sims), n - i0)
                 for j in range(len(sims)):
