@@ -411,7 +411,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         size_t bytes;
     };
     std::vector<Item> items = {
-        {(void**)&d.n_born, Np * 4}, {(void**)&d.n_dtime, Np * 4}, {(void**)&d.n_status, Np}, {(void**)&d.n_exposed, Np * 4},
+        {(void**)&d.n_born, Np * 4}, {(void**)&d.n_dtime, Np * 4}, {(void**)&d.n_next, Np * 4}, {(void**)&d.n_status, Np}, {(void**)&d.n_exposed, Np * 4},
         {(void**)&d.n_recovery, Np * 4}, {(void**)&d.n_ple, Np * 4}, {(void**)&d.n_strain, Np}, {(void**)&d.n_imm, Np},
         {(void**)&d.m_born, Mp * 4}, {(void**)&d.m_dtime, Mp * 4}, {(void**)&d.m_state, Mp}, {(void**)&d.m_exposed, Mp * 4},
         {(void**)&d.m_ple, Mp * 4}, {(void**)&d.m_strain, Mp}, {(void**)&d.ledger, (size_t)d.tiles * 4},
@@ -843,6 +843,27 @@ int arbo_sim_get_census(arbo_sim* s, arbo_census_field f, void* host, size_t byt
     return ARBO_OK;
 }
 
+// Recomputes every human's next event time from its status, times and ages (after a census write
+// that changed any of them).
+static int refresh_human_next(arbo_sim* s, void* stream)
+{
+    const Dev& d = s->d;
+    const size_t N = d.N;
+    std::vector<uint8_t> st(N);
+    std::vector<int32_t> dt(N), bn(N), ex(N), rc(N), nx(N);
+    int e;
+    if ((e = copy_out(s, st.data(), d.n_status, N, stream)) || (e = copy_out(s, dt.data(), d.n_dtime, N * 4, stream)) ||
+        (e = copy_out(s, bn.data(), d.n_born, N * 4, stream)) || (e = copy_out(s, ex.data(), d.n_exposed, N * 4, stream)) ||
+        (e = copy_out(s, rc.data(), d.n_recovery, N * 4, stream)))
+        return e;
+    for (size_t i = 0; i < N; ++i) nx[i] = human_next(st[i], dt[i], bn[i], st[i] == 1 ? ex[i] : rc[i]);
+    cudaStream_t cs = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(d.n_next, nx.data(), N * 4, cudaMemcpyHostToDevice, cs));
+    CUDA_TRY(cudaStreamSynchronize(cs));
+    s->h2d += N * 4;
+    return ARBO_OK;
+}
+
 int arbo_sim_set_census(arbo_sim* s, arbo_census_field f, const void* host, size_t bytes, void* stream)
 {
     if (!s || !host) return fail(ARBO_ERR_INVALID, "null argument");
@@ -860,6 +881,8 @@ int arbo_sim_set_census(arbo_sim* s, arbo_census_field f, const void* host, size
         CUDA_TRY(cudaMemcpyAsync(ptr, host, bytes, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         s->h2d += bytes;
+        if (f == ARBO_CENSUS_N_STATUS || f == ARBO_CENSUS_N_EXPOSED || f == ARBO_CENSUS_N_RECOVERY)
+            return refresh_human_next(s, stream);
         return ARBO_OK;
     }
     std::vector<uint8_t> cur(count);

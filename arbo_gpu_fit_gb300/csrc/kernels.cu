@@ -112,35 +112,41 @@ __device__ __forceinline__ uint32_t human_comm(const uint32_t* __restrict__ nloc
     return c;
 }
 
-// Rare per-human path, in the step that reaches time tn: a transition of an infected human or a
-// death with rebirth. `when` is the human's recovery age (status 2) or exposed age (status 1)
-// and `born` its birth time, both loaded by the caller for an infected human (its age is
-// tn - born). Returns the new status byte.
-__device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t tn, int32_t dtime, int32_t born,
-                                            int32_t when, uint32_t t, const uint32_t* __restrict__ nloc,
-                                            const uint32_t* __restrict__ hcomm, uint32_t P, const uint8_t* n_strain,
-                                            float* n_ple, int32_t* n_born, int32_t* n_dtime, uint8_t* n_imm,
-                                            uint32_t* infh, uint32_t* inc, const float* __restrict__ cdfh,
-                                            const uint32_t* __restrict__ minvh, uint32_t ah, Key key, Ctrl* ctrl)
+// Rare per-human path, in the step that reaches time tn at or after the human's next event time:
+// a transition of an exposed or infectious human or a death with rebirth. `ex` / `rec` are its
+// exposed and recovery ages and `born` its birth time (its age is tn - born). Returns the new
+// status byte in the low word and the human's new next event time in the high word.
+__device__ __noinline__ unsigned long long human_slow(uint32_t i, uint32_t st, int32_t tn, int32_t dtime, int32_t born,
+                                                      int32_t ex, int32_t rec, uint32_t t,
+                                                      const uint32_t* __restrict__ nloc,
+                                                      const uint32_t* __restrict__ hcomm, uint32_t P,
+                                                      const uint8_t* n_strain, float* n_ple, int32_t* n_born,
+                                                      int32_t* n_dtime, uint8_t* n_imm, uint32_t* infh, uint32_t* inc,
+                                                      const float* __restrict__ cdfh,
+                                                      const uint32_t* __restrict__ minvh, uint32_t ah, Key key,
+                                                      Ctrl* ctrl)
 {
+    auto pack = [](uint32_t status, int32_t next) {
+        return ((unsigned long long)(uint32_t)next << 32) | status;
+    };
     if (tn < dtime) {
         const int32_t a = tn - born;
         if (st == 2) {
-            if (when < a) {
+            if (rec < a) {
                 const uint32_t c = human_comm(nloc, hcomm, P, i);
                 counter_dec(&infh[n_strain[i] * P + c], ctrl);
-                return 0;
+                return pack(0, dtime);
             }
         } else if (st == 1) {
-            if (when < a) {
+            if (ex < a) {
                 const uint32_t c = human_comm(nloc, hcomm, P, i);
                 const uint32_t s = n_strain[i];
                 atomicAdd(&inc[s * P + c], 1u);
                 atomicAdd(&infh[s * P + c], 1u);
-                return 2;
+                return pack(2, human_next(2, dtime, born, rec));
             }
         }
-        return st;
+        return pack(st, human_next(st, dtime, born, st == 1 ? ex : rec));
     }
     if (st == 2) {
         const uint32_t c = human_comm(nloc, hcomm, P, i);
@@ -148,65 +154,55 @@ __device__ __noinline__ uint32_t human_slow(uint32_t i, uint32_t st, int32_t tn,
     }
     const U4 r = draw4(key, kHumanRebirth, i >> 2, t);
     const float ple = u01(r.v[i & 3]);
+    const int32_t dt = death_time(tn, death_age_inv(cdfh, minvh, ah, ple, 65536.0f));
     n_ple[i] = ple;
     n_born[i] = tn;
-    n_dtime[i] = death_time(tn, death_age_inv(cdfh, minvh, ah, ple, 65536.0f));
+    n_dtime[i] = dt;
     n_imm[i] = 0;
-    return 0;
+    return pack(0, dt);
 }
 
 // Human pass over groups of four (cpp/ndemographic.cu:32-105): ageing is implicit in the birth
-// times; a human dies when the new time reaches its death time, and an exposed or infectious one
-// changes status when its exposed or recovery age falls below its new age.
+// times, and each human's next event time (its death, or its exposed-to-infectious or recovery
+// step, whichever comes first) is kept up to date by every writer of its status, so the pass
+// streams only that time. A group with an event due loads its status, times and ages in one round
+// trip and takes the slow path for the humans whose event is due.
 template <int U>
 __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32_t g0, uint32_t stride, uint32_t t)
 {
-    int4 D[U];
-    uint32_t SW[U];
+    int4 X[U];
     bool ok[U];
     const int32_t tn = (int32_t)t + 1;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         const uint32_t g = g0 + u * stride;
         ok[u] = g < d.nvec;
-        if (ok[u]) {
-            D[u] = __ldcs(reinterpret_cast<const int4*>(d.n_dtime) + g);
-            SW[u] = __ldcs(reinterpret_cast<const unsigned int*>(d.n_status) + g);
-        }
+        if (ok[u]) X[u] = __ldcs(reinterpret_cast<const int4*>(d.n_next) + g);
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         if (!ok[u]) continue;
+        if (tn < X[u].x && tn < X[u].y && tn < X[u].z && tn < X[u].w) continue;  // nothing due (padding: INT_MAX)
         const uint32_t g = g0 + u * stride;
-        const int32_t dd[4] = {D[u].x, D[u].y, D[u].z, D[u].w};
-        const uint32_t sw = SW[u];
-        // A death in the group, or an exposed or infectious human in it, takes the slow path.
-        const bool dies = tn >= dd[0] || tn >= dd[1] || tn >= dd[2] || tn >= dd[3];
-        const uint32_t live = ~sw & 0x80808080u;  // bit 7 of a byte: not padding
-        const uint32_t b0 = sw & (live >> 7), b1 = (sw >> 1) & (live >> 7);
-        const uint32_t inf = (b0 ^ b1) & 0x01010101u;  // bytes with status 1 or 2
-        if (!dies && !inf) continue;
-        // Exposed and infectious humans: their exposed / recovery ages and birth times in one
-        // vector load each, so that only actual transitions take the slow path.
-        int4 E = make_int4(0, 0, 0, 0), R = E, B = E;
-        if (inf) B = reinterpret_cast<const int4*>(d.n_born)[g];
-        if (b0 & ~b1 & 0x01010101u) E = reinterpret_cast<const int4*>(d.n_exposed)[g];   // a byte == 1
-        if (b1 & ~b0 & 0x01010101u) R = reinterpret_cast<const int4*>(d.n_recovery)[g];  // a byte == 2
-        const int32_t ev[4] = {E.x, E.y, E.z, E.w}, rv[4] = {R.x, R.y, R.z, R.w}, bv[4] = {B.x, B.y, B.z, B.w};
+        const uint32_t sw = reinterpret_cast<const unsigned int*>(d.n_status)[g];
+        const int4 D = reinterpret_cast<const int4*>(d.n_dtime)[g], B = reinterpret_cast<const int4*>(d.n_born)[g];
+        const int4 E = reinterpret_cast<const int4*>(d.n_exposed)[g], R = reinterpret_cast<const int4*>(d.n_recovery)[g];
+        const int32_t xv[4] = {X[u].x, X[u].y, X[u].z, X[u].w}, dd[4] = {D.x, D.y, D.z, D.w};
+        const int32_t bv[4] = {B.x, B.y, B.z, B.w}, ev[4] = {E.x, E.y, E.z, E.w}, rv[4] = {R.x, R.y, R.z, R.w};
+        int32_t nx[4] = {xv[0], xv[1], xv[2], xv[3]};
         uint32_t nsw = sw;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
+            if (tn < xv[k]) continue;
             const uint32_t st = (sw >> (8 * k)) & 0xFFu;
-            if (st == kPad) continue;
-            const int32_t when = st == 1 ? ev[k] : rv[k];
-            if (tn < dd[k] && (st == 0 || ((st == 1 || st == 2) && !(when < tn - bv[k]))))
-                continue;  // survivor without a transition
-            const uint32_t res = human_slow(4 * g + k, st, tn, dd[k], bv[k], when, t, d.nloc, d.hcomm, d.P,
-                                            d.n_strain, d.n_ple, d.n_born, d.n_dtime, d.n_imm, d.infh, d.inc, d.cdfh,
-                                            d.minvh, d.ah, key, d.ctrl);
-            nsw = (nsw & ~(0xFFu << (8 * k))) | ((res & 0xFFu) << (8 * k));
+            const unsigned long long res =
+                human_slow(4 * g + k, st, tn, dd[k], bv[k], ev[k], rv[k], t, d.nloc, d.hcomm, d.P, d.n_strain, d.n_ple,
+                           d.n_born, d.n_dtime, d.n_imm, d.infh, d.inc, d.cdfh, d.minvh, d.ah, key, d.ctrl);
+            nsw = (nsw & ~(0xFFu << (8 * k))) | (((uint32_t)res & 0xFFu) << (8 * k));
+            nx[k] = (int32_t)(uint32_t)(res >> 32);
         }
         if (nsw != sw) reinterpret_cast<unsigned int*>(d.n_status)[g] = nsw;
+        reinterpret_cast<int4*>(d.n_next)[g] = make_int4(nx[0], nx[1], nx[2], nx[3]);
     }
 }
 
@@ -788,11 +784,12 @@ __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t k
 
 // ------------------------------------------------------------------ infection draws
 
-// Infection of human i in step t, after the demographic pass of the step. `imm` and `born` are
-// its immunity byte and birth time, loaded by the caller together with the winner key (its age
-// is t + 1 - born).
+// Infection of human i in step t, after the demographic pass of the step. `imm`, `born` and
+// `dtime` are its immunity byte, birth and death times, loaded by the caller together with the
+// winner key (its age is t + 1 - born); its next event time becomes its exposed-to-infectious
+// step or its death.
 __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t s, const U4& r, uint32_t t,
-                                             uint32_t imm, int32_t born)
+                                             uint32_t imm, int32_t born, int32_t dtime)
 {
     d.n_status[i] = 1;
     d.n_strain[i] = (uint8_t)s;
@@ -801,6 +798,7 @@ __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t 
     const int32_t ex = (int32_t)resolve(__fadd_rn((float)age, d.nExposed), r.v[0]);
     d.n_exposed[i] = ex;
     d.n_recovery[i] = (int32_t)resolve(__fadd_rn((float)ex, d.recovery), r.v[1]);
+    d.n_next[i] = human_next(1, dtime, born, ex);
 }
 
 // Target of mosquito event e: the first alive slot of its attempt sequence (dead slots are
@@ -975,7 +973,8 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
                 const uint32_t pl2 = __ffs(bal) - 1;
                 if (lane == pl2) {
                     d.winh[i] = okey;
-                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t, im, __ldcg(&d.n_born[i]));
+                    infect_human(d, i, s, draw4(key, kIntroExposed, ph, t, a), t, im, __ldcg(&d.n_born[i]),
+                                 __ldcg(&d.n_dtime[i]));
                 }
                 __syncwarp();
                 left -= 1;
@@ -1006,16 +1005,17 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
             // target writes it, so the values read here are the ones the infection needs.
             unsigned long long wk[4];
             uint32_t im[4];
-            int32_t bn[4];
+            int32_t bn[4], dt[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 wk[q] = 0;
                 im[q] = 0;
-                bn[q] = 0;
+                bn[q] = dt[q] = 0;
                 if (4 * idx + q < k) {
                     wk[q] = __ldcg(&d.winh[tg[q]]);
                     im[q] = __ldcg(&d.n_imm[tg[q]]);
                     bn[q] = __ldcg(&d.n_born[tg[q]]);
+                    dt[q] = __ldcg(&d.n_dtime[tg[q]]);
                 }
             }
 #pragma unroll
@@ -1023,7 +1023,7 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
                 const uint32_t e = 4 * idx + q;
                 if (e >= k) break;
                 if (wk[q] == order_key(hiword, j, 0, e))
-                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t, im[q], bn[q]);
+                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t, im[q], bn[q], dt[q]);
             }
         } else {
             const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
@@ -1213,6 +1213,7 @@ __global__ void k_init_humans(Dev d)
         d.n_status[j] = kPad;
         d.n_born[j] = 0;
         d.n_dtime[j] = INT_MAX;
+        d.n_next[j] = INT_MAX;
         d.n_ple[j] = 0.0f;
         d.n_strain[j] = 0;
         d.n_imm[j] = 0;
@@ -1233,9 +1234,11 @@ __global__ void k_init_humans(Dev d)
     uint32_t imm = 0;
     for (uint32_t s = 0; s < d.S; ++s)
         if (u01(dr[3 + s]) < d.seroPrev) imm |= 1u << s;
+    const int32_t dt = death_time(-age, death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f));
     d.n_born[j] = -age;  // age `age` at time 0
     d.n_ple[j] = ple;
-    d.n_dtime[j] = death_time(-age, death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f));
+    d.n_dtime[j] = dt;
+    d.n_next[j] = dt;
     d.n_status[j] = 0;
     d.n_strain[j] = 0;
     d.n_imm[j] = (uint8_t)imm;
@@ -1313,7 +1316,10 @@ __global__ void k_seed(Dev d)
         const uint32_t rr = (uint32_t)resolve(d.recovery, r.v[2]);
         const uint32_t m = rr > 1u ? rr - 1u : 1u;
         const int32_t dur = (int32_t)(bounded(r.v[1], m) + 1u);
-        d.n_recovery[i] = (d.quirks & ARBO_QUIRK_SEED_RECOVERY_DURATION) ? dur : dur - d.n_born[i];  // age + dur
+        const int32_t born = d.n_born[i];
+        const int32_t rec = (d.quirks & ARBO_QUIRK_SEED_RECOVERY_DURATION) ? dur : dur - born;  // age + dur
+        d.n_recovery[i] = rec;
+        d.n_next[i] = human_next(2, d.n_dtime[i], born, rec);
         atomicAdd(&d.infh[s * d.P + comm_of(d.nloc, d.P, i)], 1u);
     }
     if (j < d.mInit) {

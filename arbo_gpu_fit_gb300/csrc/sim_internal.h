@@ -1,8 +1,9 @@
 // sim_internal.h — device-side layout of one simulation and the kernel launchers.
 //
 // Layout in HBM (structure of arrays, every array 256-byte aligned, one allocation):
-//   humans   (N padded to a multiple of 4 agents):  birth time i32, death time i32,
-//            status u8, exposed i32, recovery i32, ple f32, strain u8, immunity u8.
+//   humans   (N padded to a multiple of 4 agents):  birth time i32, death time i32, next
+//            event time i32, status u8, exposed i32, recovery i32, ple f32, strain u8,
+//            immunity u8.
 //   mosquito (M padded to whole 128-slot tiles):     birth time i32, death time i32, state u8
 //            (bits 0-1 status, bit 7 dead), exposed i32, ple f32, strain u8; tile dead
 //            count i32 per tile. Exposed and recovery hold ages, as in the reference.
@@ -37,6 +38,17 @@ __host__ __device__ inline int32_t death_time(int32_t born, int32_t dage)
     return dage == INT_MAX ? INT_MAX : born + dage;
 }
 
+// Next demographic event time of a human of status st: its death time, or, for an exposed (1) or
+// infectious (2) human, the first step whose new age exceeds its exposed or recovery age `when`
+// (when < t - born), whichever comes first. Before that step the demographic pass has nothing to
+// do for the human.
+__host__ __device__ inline int32_t human_next(uint32_t st, int32_t dtime, int32_t born, int32_t when)
+{
+    if (st != 1 && st != 2) return dtime;
+    const int32_t tr = born + when + 1;
+    return tr < dtime ? tr : dtime;
+}
+
 constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
 constexpr uint32_t kMaxEventsPerPair = 1u << 24;
@@ -64,9 +76,10 @@ struct Dev {
     // byte and the death time of an agent and writes nothing for a survivor without a
     // transition: age at time t = t - born; the agent dies in the step that reaches time
     // t >= dtime (its age then reaches its death age; INT_MAX: never).
-    // humans
+    // humans (n_next: next demographic event time, human_next; the pass reads only this)
     int32_t* n_born;
     int32_t* n_dtime;
+    int32_t* n_next;
     uint8_t* n_status;
     int32_t* n_exposed;
     int32_t* n_recovery;

@@ -131,6 +131,16 @@ class OracleSim:
         code, dt = CENSUS[field]
         return self._view(self._lib.oracle_census, code, dt)
 
+    def set_census(self, field, values):
+        """Overwrites a census field in place (test hook, the counterpart of arbo_sim_set_census)."""
+        code, dt = CENSUS[field]
+        n = c_uint32()
+        ptr = self._lib.oracle_census(self._h, code, ctypes.byref(n))
+        v = np.ascontiguousarray(values, dt)
+        if not ptr or v.size != n.value:
+            raise ValueError(f"census {field}: expected {n.value} values")
+        ctypes.memmove(ptr, v.ctypes.data, v.nbytes)
+
     def counters(self, kind):
         dt = np.int32 if kind == "m_dead_count" else np.uint32
         return self._view(self._lib.oracle_counters, COUNTERS[kind], dt)

@@ -184,3 +184,28 @@ def test_census_ages_derived_and_read_only(gpu):
     dead = sim.census("m_dead") == 1
     assert dead.any() and np.all(sim.census("m_age")[dead] >= 0)
     compare_state(sim, orc, "after set_census")
+
+
+def test_set_census_keeps_next_events(gpu):
+    # Exposed and recovery ages written through the census move the humans' next demographic
+    # events: exposed humans whose exposed age is now in the past become infectious in the next
+    # step, infectious ones whose recovery age is in the past recover, on both sides.
+    w = small_case(seed=14, T=20)
+    sim, orc = pair(w)
+    run_and_compare(sim, orc, [6])
+    st, age = sim.census("n_status"), sim.census("n_age")
+    ex, rec = sim.census("n_exposed"), sim.census("n_recovery")
+    e1, i2 = np.flatnonzero(st == 1)[::2], np.flatnonzero(st == 2)[::2]
+    assert e1.size and i2.size
+    ex[e1] = age[e1] - 1
+    rec[i2] = age[i2] - 1
+    for side in (sim, orc):
+        side.set_census("n_exposed", ex)
+        side.set_census("n_recovery", rec)
+    sim.step(1)
+    orc.step(1)
+    compare_state(sim, orc, "after the planted transitions")
+    assert np.all(sim.census("n_status")[i2] != 2)
+    sim.step(5)
+    orc.step(5)
+    compare_state(sim, orc, "five steps later")
