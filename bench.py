@@ -35,11 +35,12 @@ sys.path.insert(0, str(ROOT))
 # Algorithmic bytes per agent-step of the demographic pass, the roofline figure: what the
 # reference's algorithm moves per agent (read age 4 + death age 4 + status 1, write age 4).
 BYTES_PER_AGENT_STEP = 13
-# What this library's layout moves instead: ages are kept as birth times, so every agent costs
-# its status byte and death time (5) and a survivor writes nothing; each birth writes the
-# newborn's PLE, birth time and death time (12) and a status byte, plus the status byte of the
-# death that freed its slot (a human's death and rebirth are one event: status and immunity).
-LAYOUT_BYTES_PER_AGENT_STEP = 5
+# What this library's layout moves instead: ages are kept as birth times, so a mosquito slot costs
+# its state byte and death time (5) and a human its next event time (4), and a survivor without a
+# transition writes nothing; each birth writes the newborn's PLE, birth time and death time (12)
+# and a status byte, plus the status byte of the death that freed its slot.
+LAYOUT_BYTES_PER_HUMAN_STEP = 4
+LAYOUT_BYTES_PER_SLOT_STEP = 5
 LAYOUT_BYTES_PER_BIRTH = 14
 FLUSH_MB = 320
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
@@ -309,7 +310,9 @@ def ours_arm(args, world, rank, local):
     demog_ms = phases[0]
     peak, peak_kind = hbm_peak()
     achieved = BYTES_PER_AGENT_STEP * w.agents / (demog_ms * 1e-3) / 1e9
-    layout_bytes = LAYOUT_BYTES_PER_AGENT_STEP * w.agents + LAYOUT_BYTES_PER_BIRTH * births
+    humans = int(w.parameter.simulation.nSize)
+    layout_bytes = (LAYOUT_BYTES_PER_HUMAN_STEP * humans + LAYOUT_BYTES_PER_SLOT_STEP * (w.agents - humans) +
+                    LAYOUT_BYTES_PER_BIRTH * births)
     layout_gbs = layout_bytes / (demog_ms * 1e-3) / 1e9
     traffic = DEMOG_TRAFFIC_BYTES * (w.agents / 7_000_000) if DEMOG_TRAFFIC_BYTES else None
 
@@ -340,7 +343,8 @@ def ours_arm(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_demog", "peak_kind": peak_kind,
                      "bytes_per_agent_step": BYTES_PER_AGENT_STEP, "kernel_ms": demog_ms,
-                     "layout": {"bytes": layout_bytes, "bytes_per_agent_step": LAYOUT_BYTES_PER_AGENT_STEP,
+                     "layout": {"bytes": layout_bytes, "bytes_per_human_step": LAYOUT_BYTES_PER_HUMAN_STEP,
+                                "bytes_per_slot_step": LAYOUT_BYTES_PER_SLOT_STEP,
                                 "bytes_per_birth": LAYOUT_BYTES_PER_BIRTH, "births_per_step": births,
                                 "achieved": layout_gbs, "frac": layout_gbs / peak},
                      "phase_ms": {"demographic": phases[0], "foi_series": phases[1], "infection": phases[2],
