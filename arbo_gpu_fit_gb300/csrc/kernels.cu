@@ -1,20 +1,20 @@
 // kernels.cu — sm_103a kernels of one simulation time step and of its initialisation.
 //
 // One step is three launches (captured in a CUDA graph by the host):
-//   k_demog   human and mosquito demographic passes over the whole census (HBM stream:
-//             read status and death time; ages are birth times, so a survivor without a
-//             transition writes nothing), per-tile mosquito recruitment,
-//             counter deltas; replaces nBlockBirthDeath + resetIncidence + mBlockBirthDeath
-//             (cpp/ndemographic.cu:32-120, cpp/mdemographic.cu:22-150).
+//   k_demog   human and mosquito demographic passes over the whole census (HBM stream: a
+//             human's next event time, a mosquito slot's state byte and death time; ages are
+//             birth times, so a survivor without a transition writes nothing), per-tile
+//             mosquito recruitment, counter deltas; replaces nBlockBirthDeath + resetIncidence
+//             + mBlockBirthDeath (cpp/ndemographic.cu:32-120, cpp/mdemographic.cu:22-150).
 //   k_foi     per (serotype, community): the series row of the next time point, then the
 //             force of infection both ways with stay / long-distance / CSR-local dispersal;
 //             replaces dataCollect + initialTransmission + nVisitingInfected +
 //             mVisitingInfected (cpp/datacollect.cu:10-189, cpp/epidemic.cu:12-29,
 //             cpp/nepidemic.cu:28-142, cpp/mepidemic.cu:28-138).
-//   k_infect  per community: event-parallel infection draws resolved to the reference's
-//             serial order by a minimum order key per target, external introductions,
-//             application of the winners; replaces nmTransmission + mnTransmission
-//             (cpp/mepidemic.cu:143-246, cpp/nepidemic.cu:146-319).
+//   k_infect  one warp per community: event-parallel infection draws resolved to the
+//             reference's serial order by a minimum order key per target, external
+//             introductions, application of the winners; replaces nmTransmission +
+//             mnTransmission (cpp/mepidemic.cu:143-246, cpp/nepidemic.cu:146-319).
 // No tensor cores: the work is integer streaming and scattered events.
 #include <cuda_runtime.h>
 

@@ -47,8 +47,8 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # Per-launch DRAM traffic of the demographic kernel on this workload, from the ncu capture
 # summarised in profiles/k_demog_plain_large.md: dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch (44,204,032 + 8,091,392 bytes).
-DEMOG_TRAFFIC_BYTES = 52_295_424
+# one launch (42,423,296 + 7,979,008 bytes).
+DEMOG_TRAFFIC_BYTES = 50_402_304
 
 
 def parse():
