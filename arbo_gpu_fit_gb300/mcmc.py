@@ -307,7 +307,7 @@ def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np
     returns an approximate log-likelihood per chain. Stage 1 screens every proposal with it (GPU,
     FP64); only the proposals that pass are simulated, together in one batch of as many handles as
     there are passing chains (replicates each), and stage 2 accepts them with the simulator's
-    likelihood divided by the surrogate's. The simulator stays the judge: a proposal is accepted
+    likelihood divided by the surrogate's. The simulator has the last word: a proposal is accepted
     only on its simulated likelihood."""
     sims = sims if sims is not None else m.make_sims(m.C * m.R)
     t0 = time.perf_counter()
