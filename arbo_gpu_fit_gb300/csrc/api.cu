@@ -285,6 +285,28 @@ int arbo_community_sizes(const double* w, uint32_t P, uint32_t total, uint32_t* 
     return ARBO_OK;
 }
 
+// Rates and shapes the kernels and tables rely on (the reference checked none: a NaN or negative
+// rate there gives silent garbage). Returns the first violation, or nullptr.
+static const char* param_error(const arbo_sim_param& p, uint32_t N, uint32_t M)
+{
+    auto finite = [](float x) { return std::isfinite(x); };
+    const float probs[] = {p.mnBitingSuccess, p.nmBitingSuccess, p.longDistance, p.noDistance, p.initialSeroPrev};
+    for (float x : probs)
+        if (!(x >= 0.0f && x <= 1.0f)) return "transmission, dispersal and seroprevalence probabilities must be in [0, 1]";
+    const float nonneg[] = {p.bitingRate, p.recovery, p.mExposed, p.nExposed, p.externalInfection,
+                            p.nInitialInf, p.mInitialInf, p.mosBaseRatio, p.nLocWeibull};
+    for (float x : nonneg)
+        if (!(x >= 0.0f) || !finite(x)) return "rates, durations, seed counts and mosBaseRatio must be finite and >= 0";
+    const float pos[] = {p.nShapeInfantMortality, p.nScaleInfantMortality, p.nScaleLifeExpectancy,
+                         p.nShapeLifeExpectancy, p.mScaleLifeExpectancy, p.mShapeLifeExpectancy};
+    for (float x : pos)
+        if (!(x > 0.0f) || !finite(x)) return "life-expectancy shapes and scales must be finite and > 0";
+    if (!finite(p.seasonAmp) || !finite(p.seasonPhase) || !finite(p.nHeteroPopSize) || !finite(p.mHeteroPopSize))
+        return "seasonal and community-size parameters must be finite";
+    if (p.nInitialInf > (float)N || p.mInitialInf > (float)M) return "more initial infections than agents";
+    return nullptr;
+}
+
 int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const arbo_io_param* io, const arbo_csr* csr,
                     const uint32_t* n_comm_size, const uint32_t* m_comm_size, uint32_t max_time, uint64_t seed,
                     uint32_t instance, arbo_sim** out)
@@ -305,6 +327,7 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     if (p.maxTargetAttempt < 1 || p.maxTargetAttempt > (1u << 18))
         return fail(ARBO_ERR_INVALID, "maxTargetAttempt must be in [1, 2^18]");
     if (p.maxIntroAttempt > (1u << 26)) return fail(ARBO_ERR_INVALID, "maxIntroAttempt must be <= 2^26");
+    if (const char* why = param_error(p, N, M)) return fail(ARBO_ERR_INVALID, why);
     if (!csr->loc || (csr->nnz && !csr->to) || csr->loc[0] != 0 || csr->loc[P] != csr->nnz)
         return fail(ARBO_ERR_INVALID, "malformed CSR (loc[0] must be 0 and loc[P] == nnz)");
     for (uint32_t c = 0; c < P; ++c)
@@ -319,6 +342,11 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
         arch.infectBlock % 32)
         return fail(ARBO_ERR_INVALID, "launch knobs: demogBlock in [32, 256], foiBlock and infectBlock in [32, 512], "
                                       "all multiples of 32; demogUnroll 1, 2 or 4");
+    if (n_comm_size && m_comm_size) {
+        uint64_t sn = 0, sm = 0;
+        for (uint32_t c = 0; c < P; ++c) sn += n_comm_size[c], sm += m_comm_size[c];
+        if (sn != N || sm != M) return fail(ARBO_ERR_INVALID, "community sizes must sum to nSize and mSize");
+    }
 
     arbo_sim* s = new arbo_sim();
     s->p = p;
@@ -332,16 +360,9 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     s->nsize.resize(P);
     s->msize.resize(P);
     if (n_comm_size && m_comm_size) {
-        uint64_t sn = 0, sm = 0;
         for (uint32_t c = 0; c < P; ++c) {
             s->nsize[c] = n_comm_size[c];
             s->msize[c] = m_comm_size[c];
-            sn += n_comm_size[c];
-            sm += m_comm_size[c];
-        }
-        if (sn != N || sm != M) {
-            delete s;
-            return fail(ARBO_ERR_INVALID, "community sizes must sum to nSize and mSize");
         }
     } else {
         std::vector<double> wn(P), wm(P);
@@ -552,6 +573,7 @@ int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p)
                                       "and attempt parameters; sizes and life expectancies need a new handle");
     if (p->maxTargetAttempt < 1 || p->maxTargetAttempt > (1u << 18) || p->maxIntroAttempt > (1u << 26))
         return fail(ARBO_ERR_INVALID, "attempt limits out of range");
+    if (const char* why = param_error(*p, s->d.N, s->d.M)) return fail(ARBO_ERR_INVALID, why);
     CUDA_TRY(cudaSetDevice(s->device));
     CUDA_TRY(cudaDeviceSynchronize());  // no step of this handle may be reading the old series
     s->p = *p;

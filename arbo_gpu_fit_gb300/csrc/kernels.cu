@@ -680,9 +680,19 @@ __device__ __forceinline__ void foi_block(const Dev& d, uint32_t b, int collect_
                 rm = draw4(key, kFoiMH, p, t);
             }
             griddep_wait();
-            const uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
-            const uint32_t mcc = d.mcnt[c];
+            uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
+            uint32_t mcc = d.mcnt[c];
             if (ic) d.inc[p] = 0u;
+            // A count at or above 2^31 is a counter that went below zero (counter_dec records
+            // ARBO_DEVERR_COUNTER when that happens): it is read as 0, so that an inconsistent
+            // state cannot turn into an unbounded number of events.
+            if ((ih | im | ic | mcc) & 0x80000000u) {
+                atomicOr(&d.ctrl->err, ARBO_DEVERR_COUNTER);
+                ih = (ih & 0x80000000u) ? 0u : ih;
+                im = (im & 0x80000000u) ? 0u : im;
+                ic = (ic & 0x80000000u) ? 0u : ic;
+                mcc = (mcc & 0x80000000u) ? 0u : mcc;
+            }
             if (ih) atomicAdd(&s_sum[s], ih);
             if (ic) atomicAdd(&s_sum[ARBO_MAX_STRAINS + s], ic);
             if (im) atomicAdd(&s_sum[2 * ARBO_MAX_STRAINS + s], im);

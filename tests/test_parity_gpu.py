@@ -209,3 +209,24 @@ def test_set_census_keeps_next_events(gpu):
     sim.step(5)
     orc.step(5)
     compare_state(sim, orc, "five steps later")
+
+
+def test_device_error_word_reports_inconsistent_counters(gpu):
+    # A fault injected from the host: the infectious-human counters are zeroed while infectious
+    # humans exist, so their recoveries would take the counters below zero. The kernels record
+    # ARBO_DEVERR_COUNTER in the device error word (no trap, the context stays usable), status()
+    # reports it and run() refuses to report success; a fresh init clears it.
+    from arbo_gpu_fit_gb300 import _native
+
+    w = small_case(seed=19, T=40)
+    sim, orc = pair(w)
+    run_and_compare(sim, orc, [10])
+    assert (sim.census("n_status") == 2).any()
+    sim.set_counters("n_infected_subpop", np.zeros_like(sim.counters("n_infected_subpop")))
+    with pytest.raises(_native.ArboError):
+        sim.run()
+    err, _ = sim.status()
+    assert err & _native.DEVERR_COUNTER
+    sim.init()
+    sim.step(3)
+    assert sim.status()[0] == 0
