@@ -814,12 +814,14 @@ __device__ __forceinline__ void infect_human(const Dev& d, uint32_t i, uint32_t 
 // Target of mosquito event e: the first alive slot of its attempt sequence (dead slots are
 // retried, cpp/mepidemic.cu:206-235). Returns UINT_MAX when the attempts run out. The four
 // candidates of one Philox call are loaded together (one memory round trip) and the first alive
-// one in attempt order is taken; its state byte is left in *state.
+// one in attempt order is taken; its state byte is left in *state. `first` is the draw of the
+// first four attempts (the caller computes it together with other lanes' draws).
 __device__ __forceinline__ uint32_t mosquito_target(const Dev& d, const Key& key, uint32_t pidx, uint32_t e,
-                                                    uint32_t base, uint32_t size, uint32_t t, uint32_t* state)
+                                                    uint32_t base, uint32_t size, uint32_t t, uint32_t* state,
+                                                    const U4& first)
 {
     for (uint32_t a = 0; a < d.maxTarget; a += 4) {
-        const U4 r = draw4(key, kInfMTarget, pidx, t, e, a >> 2);
+        const U4 r = a == 0 ? first : draw4(key, kInfMTarget, pidx, t, e, a >> 2);
         uint32_t slot[4], st[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) slot[q] = base + bounded(r.v[q], size);
@@ -883,10 +885,9 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
     const uint32_t ns = __ldg(&d.nsize[c]), ms = __ldg(&d.msize[c]);
     const uint32_t nbase = __ldg(&d.nloc[c]), mbase = __ldg(&d.mloc[c]);
     const uint32_t pl = lane * P + c;
-    U4 rd;
-    if (lane < S) rd = draw4(key, kIntroCount, pl, t);
-    else if (lane == 8) rd = draw4(key, kInfMStart, c, t);
-    else if (lane == 9) rd = draw4(key, kInfHStart, c, t);
+    // One draw per lane in one pass: introduction counts (lanes < S), first serotypes (8, 9).
+    const U4 rd = draw4(key, lane < S ? (uint32_t)kIntroCount : lane == 8 ? (uint32_t)kInfMStart : (uint32_t)kInfHStart,
+                        lane < S ? pl : c, t);
     griddep_wait();
     const uint32_t mc = d.mcnt[c];
     uint32_t kh = lane < S ? d.transh[pl] : 0u;
@@ -927,12 +928,17 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
     const bool any_intro = __any_sync(kFull, ne != 0);
     if (items == 0 && !any_intro) return;
 
-    // Phase A
+    // Phase A. Human groups and mosquito events draw their targets in one pass (the first four
+    // attempts of a mosquito event).
     for (uint32_t it = lane; it < items; it += 32) {
-        if (it < H) {
-            const uint32_t j = item_position(sh.hstart, S, it), idx = it - sh.hstart[j];
-            const uint32_t s = (s0h + j) % S, ph = s * P + c, k = sh.kh[j];
-            const U4 r = draw4(key, kInfHTarget, ph, t, idx);
+        const bool hum = it < H;
+        const uint32_t rel = hum ? it : it - H;
+        const uint32_t j = item_position(hum ? sh.hstart : sh.mstart, S, rel);
+        const uint32_t idx = rel - (hum ? sh.hstart[j] : sh.mstart[j]);
+        const uint32_t sp = ((hum ? s0h : s0m) + j) % S, pp = sp * P + c;
+        const U4 r = draw4(key, hum ? (uint32_t)kInfHTarget : (uint32_t)kInfMTarget, pp, t, idx);
+        if (hum) {
+            const uint32_t s = sp, k = sh.kh[j];
             uint32_t tg[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) tg[q] = nbase + bounded(r.v[q], ns);
@@ -945,10 +951,8 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
                 if (st == 0 && !((im >> s) & 1u)) atomicMin(&d.winh[tg[q]], order_key(hiword, j, 0, e));
             }
         } else {
-            const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
-            const uint32_t sm = (s0m + j) % S, pm = sm * P + c;
             uint32_t st = 0;
-            const uint32_t slot = mosquito_target(d, key, pm, idx, mbase, ms, t, &st);
+            const uint32_t slot = mosquito_target(d, key, pp, idx, mbase, ms, t, &st, r);
             if (it < kTargetCache) sh.target[it].x = slot;
             if (slot == UINT_MAX) atomicAdd(&d.ctrl->diag[0], 1u);
             else if (st == 0) atomicMin(&d.winm[slot], order_key(hiword, j, 0, idx));
@@ -1039,7 +1043,9 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
             const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
             const uint32_t sm = (s0m + j) % S, pm = sm * P + c;
             uint32_t st = 0;
-            const uint32_t slot = it < kTargetCache ? sh.target[it].x : mosquito_target(d, key, pm, idx, mbase, ms, t, &st);
+            const uint32_t slot = it < kTargetCache
+                                      ? sh.target[it].x
+                                      : mosquito_target(d, key, pm, idx, mbase, ms, t, &st, draw4(key, kInfMTarget, pm, t, idx));
             unsigned long long wk = 0;
             int32_t bn = 0;
             if (slot != UINT_MAX) {  // winner key and birth time in one round trip
