@@ -156,9 +156,36 @@ def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt
     return out
 
 
+def time_batch(population: str, instances: int, steps: int, warm: int) -> dict:
+    """Per-phase times of one batch of the chains' handles (the batched fit's simulation step):
+    `instances` handles of the workload with seeds seed..seed+instances-1, `warm` untimed steps,
+    then `steps` steps timed phase by phase (CUDA events)."""
+    from .mcmc import chain_batch
+    from .simulation import Simulation
+
+    w = workload(population)
+    sims = [Simulation(w.parameter, w.network, w.n_sizes, w.m_sizes, max_time=w.max_time, seed=w.seed + k)
+            for k in range(instances)]
+    b = chain_batch(sims)
+    try:
+        b.init()
+        b.step(warm)
+        ph = b.time_phases(steps)
+        arch, grids = b.arch()
+        return {"population": population, "instances": instances, "warm_steps": warm, "steps": steps,
+                "phase_us": {"demographic": ph[0] * 1e3, "foi_series": ph[1] * 1e3, "infection": ph[2] * 1e3,
+                             "step": ph[3] * 1e3},
+                "shape": [arch.demogBlock, arch.demogUnroll, arch.foiBlock, arch.infectBlock], "grids": list(grids)}
+    finally:
+        b.close()
+        for s in sims:
+            s.close()
+
+
 def main(argv=None):
     """python -m arbo_gpu_fit_gb300.fit --population small --iters 300 --adapt 100 --plain-iters 20
-    --train-runs 4096 --epochs 60 [--out result.json]"""
+    --train-runs 4096 --epochs 60 [--out result.json]; with --time-batch N, only the per-phase
+    times of one batch of N handles (--time-steps steps after --warm-steps)."""
     import argparse
     import json
 
@@ -176,8 +203,14 @@ def main(argv=None):
     ap.add_argument("--replicates", type=int, default=1, help="simulations per proposal (log-mean-exp)")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--time-batch", type=int, default=0, help="time one batch of this many handles and exit")
+    ap.add_argument("--time-steps", type=int, default=2)
+    ap.add_argument("--warm-steps", type=int, default=160)
     a = ap.parse_args(argv)
     _native.check(_native.load().arbo_set_device(a.device))
+    if a.time_batch:
+        print(json.dumps(time_batch(a.population, a.time_batch, a.time_steps, a.warm_steps)))
+        return
     t0 = time.perf_counter()
     r = compare(a.population, chains=a.chains, iters=a.iters, adapt_until=a.adapt, plain_iters=a.plain_iters,
                 train_runs=a.train_runs, epochs=a.epochs, step_fraction=a.step_fraction,
