@@ -1261,7 +1261,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
         const Dev& d = b->sims[i]->d;
         const uint64_t hb = cdiv(d.nvec, (uint64_t)32 * a.demogUnroll);  // warp items
         const uint64_t mb = cdiv(d.tiles, kQuad);
-        const uint64_t fb = cdiv((uint64_t)d.S * d.P, a.foiBlock / 4);
+        const uint64_t fb = cdiv((uint64_t)d.S * d.P, 32);  // force of infection: warps of 32 pairs
         const uint64_t ib = d.P;  // the infection kernel takes communities, one warp each
         if (demog_off[i] + hb + mb >= (1ull << 31) || foi_off[i] + fb >= (1ull << 31) ||
             infect_off[i] + ib >= (1ull << 31))
@@ -1304,7 +1304,9 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     b->blocks[1] = foi_off[n];
     b->blocks[2] = infect_off[n];
     bd.grid_demog = std::max(1u, std::min(b->blocks[0], l.numSM * occ[0]));
-    bd.grid_foi = std::max(1u, std::min(b->blocks[1], l.numSM * occ[1]));
+    const uint32_t fwarps = l.numSM * occ[1] * (a.foiBlock / 32);
+    bd.foi_run = std::max(1u, std::min(kInfectRunMax, b->blocks[1] / std::max(fwarps, 1u)));
+    bd.grid_foi = std::max(1u, std::min(cdiv(cdiv(b->blocks[1], bd.foi_run), a.foiBlock / 32), l.numSM * occ[1]));
     // Runs of consecutive communities per warp (fewer descriptor restagings), as long as every
     // resident warp still gets one.
     const uint32_t warps = l.numSM * occ[2] * K;

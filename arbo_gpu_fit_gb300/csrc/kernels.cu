@@ -637,159 +637,158 @@ __device__ __forceinline__ void split_events(const Dev& d, uint32_t* trans, floa
     *nlong = lng;
 }
 
-// Series row + force of infection. A CTA of 4*K threads owns K consecutive (serotype,
-// community) pairs: K threads read the counters, add the series sums and split each pair's
-// events; then all threads spread the flattened events of the K pairs, four per Philox call.
-struct FoiSmem {
-    uint32_t cnt[512], scan[513], loc[128], deg[128], sum[3 * ARBO_MAX_STRAINS + 2], wt[16];
-    uint32_t to[128][8];  // CSR row of each pair's source community (degree <= 8)
+// Series row + force of infection, by one warp for 32 consecutive (serotype, community) pairs,
+// one per lane: each lane reads its pair's counters, adds them to the warp's series sums and
+// splits the pair's events both ways; then the 32 lanes spread the flattened events of the warp's
+// 128 (pair, kind) entries, four per Philox call. No block barrier: a warp is a chain of two
+// dependent round trips and its draws, so the more warps in flight the better.
+struct __align__(16) FoiWarpSmem {
+    uint32_t to[32][8];                      // CSR row of each lane's source community (degree <= 8)
+    uint32_t cnt[32][4];                     // events of (lane, kind): 0 HM local, 1 HM long, 2 MH local, 3 MH long
+    uint32_t kofs[32][4];                    // first group of four of (lane, kind) in the warp's space
+    uint32_t base[33];                       // first group of each lane; base[32] = groups in the warp
+    uint32_t loc[32], deg[32];
+    uint32_t sum[3 * ARBO_MAX_STRAINS + 2];  // series sums: infected, incidence, infectious mosquitoes; humans, mosquitoes
 };
 
-__device__ __forceinline__ void foi_block(const Dev& d, uint32_t b, int collect_only, uint32_t koff, FoiSmem& fs)
+__device__ __forceinline__ void foi_warp(const Dev& d, uint32_t p0, int collect_only, uint32_t koff, FoiWarpSmem& sh)
 {
-    uint32_t* const s_cnt = fs.cnt;
-    uint32_t* const s_scan = fs.scan;
-    uint32_t* const s_loc = fs.loc;
-    uint32_t* const s_deg = fs.deg;
-    uint32_t* const s_sum = fs.sum;
-    uint32_t* const s_wt = fs.wt;
-    uint32_t(*const s_to)[8] = fs.to;
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
     const uint32_t row = collect_only ? 0u : t + 1;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t K = blockDim.x >> 2;
     const uint32_t SP = d.S * d.P, S = d.S, P = d.P;
-    const uint32_t p0 = b * K;
-    if (tid < 3 * ARBO_MAX_STRAINS + 2) s_sum[tid] = 0;
-    __syncthreads();
+    const uint32_t p = p0 + lane;
+    const bool valid = p < SP;
+    if (lane < 3 * ARBO_MAX_STRAINS + 2) sh.sum[lane] = 0;
     uint32_t nk[4] = {0, 0, 0, 0};
-    if (tid < K) {
-        const uint32_t p = p0 + tid;
-        if (p < SP) {
-            // Loads of static data and the keyed draws run before the wait on the demographic
-            // kernel (programmatic dependent launch); the counters it writes are read after.
-            const uint32_t s = p / P, c = p - s * P;
-            const uint32_t ncc = __ldg(&d.ncnt[c]);
-            const uint32_t loc = __ldg(&d.csr_loc[c]), loc1 = __ldg(&d.csr_loc[c + 1]);
-            if (!collect_only && loc1 - loc <= 8)
-                for (uint32_t q = 0; q < loc1 - loc; ++q) s_to[tid][q] = __ldg(&d.csr_to[loc + q]);
-            U4 rh, rm;
-            if (!collect_only) {
-                rh = draw4(key, kFoiHM, p, t);
-                rm = draw4(key, kFoiMH, p, t);
-            }
-            griddep_wait();
-            uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
-            uint32_t mcc = d.mcnt[c];
-            if (ic) d.inc[p] = 0u;
-            // A count at or above 2^31 is a counter that went below zero (counter_dec records
-            // ARBO_DEVERR_COUNTER when that happens): it is read as 0, so that an inconsistent
-            // state cannot turn into an unbounded number of events.
-            if ((ih | im | ic | mcc) & 0x80000000u) {
-                atomicOr(&d.ctrl->err, ARBO_DEVERR_COUNTER);
-                ih = (ih & 0x80000000u) ? 0u : ih;
-                im = (im & 0x80000000u) ? 0u : im;
-                ic = (ic & 0x80000000u) ? 0u : ic;
-                mcc = (mcc & 0x80000000u) ? 0u : mcc;
-            }
-            if (ih) atomicAdd(&s_sum[s], ih);
-            if (ic) atomicAdd(&s_sum[ARBO_MAX_STRAINS + s], ic);
-            if (im) atomicAdd(&s_sum[2 * ARBO_MAX_STRAINS + s], im);
-            if (c == 0) d.s_one[row * S + s] = ih;
-            if (s == 0) {
-                atomicAdd(&s_sum[3 * ARBO_MAX_STRAINS], ncc);
-                atomicAdd(&s_sum[3 * ARBO_MAX_STRAINS + 1], mcc);
-            }
-            if (d.recordSpatial) d.s_spatial[(size_t)row * SP + p] = ih;
-            if (!collect_only && (ih | im)) {
-                const uint32_t deg = loc1 - loc;
-                s_loc[tid] = loc;
-                s_deg[tid] = deg;
-                if (ih > 0) {  // human -> mosquito (cpp/nepidemic.cu:28-142)
-                    const float ratio = __fdiv_rn((float)mcc, (float)ncc);
-                    float x = __fmul_rn(ratio, d.biting);
-                    x = __fmul_rn(x, d.nmSuccess);
-                    x = __fmul_rn(x, (float)ih);
-                    split_events(d, d.transm, x, rh, p, deg, &nk[0], &nk[1]);
-                }
-                if (im > 0) {  // mosquito -> human (cpp/mepidemic.cu:28-138)
-                    float x = __fmul_rn(d.biting, d.mnSuccess);
-                    x = __fmul_rn(x, (float)im);
-                    split_events(d, d.transh, x, rm, p, deg, &nk[2], &nk[3]);
-                }
-            }
+    uint32_t s = 0, c = 0, ncc = 0, loc = 0, deg = 0;
+    U4 rh, rm;
+    if (valid) {
+        // Loads of static data and the keyed draws run before the wait on the demographic kernel
+        // (programmatic dependent launch); the counters it writes are read after.
+        s = p / P;
+        c = p - s * P;
+        ncc = __ldg(&d.ncnt[c]);
+        loc = __ldg(&d.csr_loc[c]);
+        deg = __ldg(&d.csr_loc[c + 1]) - loc;
+        if (!collect_only && deg <= 8)
+            for (uint32_t q = 0; q < deg; ++q) sh.to[lane][q] = __ldg(&d.csr_to[loc + q]);
+        if (!collect_only) {
+            rh = draw4(key, kFoiHM, p, t);
+            rm = draw4(key, kFoiMH, p, t);
         }
     }
     griddep_wait();
-    // s_cnt[4*pair + kind] for kind 0 HM local, 1 HM long, 2 MH local, 3 MH long
-    if (tid < K) {
-#pragma unroll
-        for (int kd = 0; kd < 4; ++kd) s_cnt[4 * tid + kd] = nk[kd];
+    __syncwarp();  // the sums are zeroed
+    if (valid) {
+        uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
+        uint32_t mcc = d.mcnt[c];
+        if (ic) d.inc[p] = 0u;
+        // A count at or above 2^31 is a counter that went below zero (counter_dec records
+        // ARBO_DEVERR_COUNTER when that happens): it is read as 0, so that an inconsistent state
+        // cannot turn into an unbounded number of events.
+        if ((ih | im | ic | mcc) & 0x80000000u) {
+            atomicOr(&d.ctrl->err, ARBO_DEVERR_COUNTER);
+            ih = (ih & 0x80000000u) ? 0u : ih;
+            im = (im & 0x80000000u) ? 0u : im;
+            ic = (ic & 0x80000000u) ? 0u : ic;
+            mcc = (mcc & 0x80000000u) ? 0u : mcc;
+        }
+        if (ih) atomicAdd(&sh.sum[s], ih);
+        if (ic) atomicAdd(&sh.sum[ARBO_MAX_STRAINS + s], ic);
+        if (im) atomicAdd(&sh.sum[2 * ARBO_MAX_STRAINS + s], im);
+        if (c == 0) d.s_one[row * S + s] = ih;
+        if (s == 0) {
+            atomicAdd(&sh.sum[3 * ARBO_MAX_STRAINS], ncc);
+            atomicAdd(&sh.sum[3 * ARBO_MAX_STRAINS + 1], mcc);
+        }
+        if (d.recordSpatial) d.s_spatial[(size_t)row * SP + p] = ih;
+        if (!collect_only && (ih | im)) {
+            if (ih > 0) {  // human -> mosquito (cpp/nepidemic.cu:28-142)
+                const float ratio = __fdiv_rn((float)mcc, (float)ncc);
+                float x = __fmul_rn(ratio, d.biting);
+                x = __fmul_rn(x, d.nmSuccess);
+                x = __fmul_rn(x, (float)ih);
+                split_events(d, d.transm, x, rh, p, deg, &nk[0], &nk[1]);
+            }
+            if (im > 0) {  // mosquito -> human (cpp/mepidemic.cu:28-138)
+                float x = __fmul_rn(d.biting, d.mnSuccess);
+                x = __fmul_rn(x, (float)im);
+                split_events(d, d.transh, x, rm, p, deg, &nk[2], &nk[3]);
+            }
+        }
     }
-    __syncthreads();
-    if (tid < 3 * S) {
-        const uint32_t kind = tid / S, s = tid - kind * S;
-        const uint32_t v = s_sum[kind * ARBO_MAX_STRAINS + s];
+    __syncwarp();
+    if (lane < 3 * S) {
+        const uint32_t kind = lane / S, ss = lane - kind * S;
+        const uint32_t v = sh.sum[kind * ARBO_MAX_STRAINS + ss];
         uint32_t* dst = kind == 0 ? d.s_ninf : kind == 1 ? d.s_ninc : d.s_minf;
-        if (v) atomicAdd(&dst[row * S + s], v);
-    } else if (tid == 3 * S) {
-        if (s_sum[3 * ARBO_MAX_STRAINS]) atomicAdd(&d.s_ncount[row], s_sum[3 * ARBO_MAX_STRAINS]);
-        if (s_sum[3 * ARBO_MAX_STRAINS + 1]) atomicAdd(&d.s_mcount[row], s_sum[3 * ARBO_MAX_STRAINS + 1]);
+        if (v) atomicAdd(&dst[row * S + ss], v);
+    } else if (lane == 3 * S) {
+        if (sh.sum[3 * ARBO_MAX_STRAINS]) atomicAdd(&d.s_ncount[row], sh.sum[3 * ARBO_MAX_STRAINS]);
+        if (sh.sum[3 * ARBO_MAX_STRAINS + 1]) atomicAdd(&d.s_mcount[row], sh.sum[3 * ARBO_MAX_STRAINS + 1]);
     }
-    if (collect_only) return;
-    griddep_launch_dependents();
-    // Exclusive scan of the groups of four events of every (pair, kind) entry.
-    uint32_t v = (s_cnt[tid] + 3) >> 2;
-    const uint32_t own = v;
+    if (collect_only) {
+        __syncwarp();  // the sums are read before the warp's next pairs zero them
+        return;
+    }
+    // Groups of four events: per lane over its four kinds, then an exclusive scan over the lanes.
+    uint32_t own = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        sh.cnt[lane][k] = nk[k];
+        sh.kofs[lane][k] = own;
+        own += (nk[k] + 3) >> 2;
+    }
+    sh.loc[lane] = loc;
+    sh.deg[lane] = deg;
+    uint32_t v = own;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
         const uint32_t y = __shfl_up_sync(kFull, v, off);
         if (lane >= (uint32_t)off) v += y;
     }
-    if (lane == 31) s_wt[warp] = v;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t acc = 0;
-        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
-            const uint32_t x = s_wt[w];
-            s_wt[w] = acc;
-            acc += x;
-        }
-        s_scan[blockDim.x] = acc;
-    }
-    __syncthreads();
-    s_scan[tid] = v - own + s_wt[warp];
-    __syncthreads();
-    const uint32_t G = s_scan[blockDim.x];
-    for (uint32_t gi = tid; gi < G; gi += blockDim.x) {
-        uint32_t lo = 0, hi = blockDim.x - 1;  // last entry with s_scan[entry] <= gi
+    sh.base[lane] = v - own;
+    if (lane == 31) sh.base[32] = v;
+    __syncwarp();
+    const uint32_t G = sh.base[32];
+    for (uint32_t gi = lane; gi < G; gi += 32) {
+        uint32_t lo = 0, hi = 31;  // last lane whose first group is <= gi
         while (lo < hi) {
             const uint32_t mid = (lo + hi + 1) >> 1;
-            if (s_scan[mid] <= gi) lo = mid; else hi = mid - 1;
+            if (sh.base[mid] <= gi) lo = mid; else hi = mid - 1;
         }
-        const uint32_t entry = lo, pair = entry >> 2, kind = entry & 3u;
-        const uint32_t r4 = gi - s_scan[entry];
-        const uint32_t p = p0 + pair, s = p / P;
-        const uint32_t n = s_cnt[entry];
+        const uint32_t owner = lo, rel = gi - sh.base[owner];
+        const uint32_t kind = rel >= sh.kofs[owner][3] ? 3u : rel >= sh.kofs[owner][2] ? 2u : rel >= sh.kofs[owner][1] ? 1u : 0u;
+        const uint32_t r4 = rel - sh.kofs[owner][kind];
+        const uint32_t po = p0 + owner, so = po / P;
+        const uint32_t n = sh.cnt[owner][kind];
         const uint32_t stream = kind == 0 ? kFoiHMLocal : kind == 1 ? kFoiHMLong : kind == 2 ? kFoiMHLocal : kFoiMHLong;
         uint32_t* trans = kind < 2 ? d.transm : d.transh;
-        const U4 r = draw4(key, stream, p, t, r4);
-        const uint32_t loc = s_loc[pair], deg = s_deg[pair];
+        const U4 r = draw4(key, stream, po, t, r4);
+        const uint32_t lo_ = sh.loc[owner], dg = sh.deg[owner];
 #pragma unroll
         for (int qq = 0; qq < 4; ++qq) {
             if (4 * r4 + qq >= n) break;
-            const uint32_t nb = (kind & 1u) ? 0u : bounded(r.v[qq], deg);
-            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : (deg <= 8 ? s_to[pair][nb] : __ldg(&d.csr_to[loc + nb]));
-            atomicAdd(&trans[s * P + dest], 1u);
+            const uint32_t nb = (kind & 1u) ? 0u : bounded(r.v[qq], dg);
+            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : (dg <= 8 ? sh.to[owner][nb] : __ldg(&d.csr_to[lo_ + nb]));
+            atomicAdd(&trans[so * P + dest], 1u);
         }
     }
+    __syncwarp();  // the tables are reused for the warp's next pairs
 }
 
+// Warp w of block b takes pairs 32 * (b * W + w), then every gridDim.x * W warps further
+// (W = blockDim.x / 32; W per-warp tables in dynamic shared memory).
 __global__ void __launch_bounds__(512) k_foi(Dev d, int collect_only, uint32_t koff)
 {
-    __shared__ FoiSmem fs;
-    foi_block(d, blockIdx.x, collect_only, koff, fs);
+    extern __shared__ __align__(16) unsigned char foi_dyn[];
+    const uint32_t warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    FoiWarpSmem& sh = reinterpret_cast<FoiWarpSmem*>(foi_dyn)[warp];
+    const uint32_t SP = d.S * d.P;
+    griddep_launch_dependents();  // the infection kernel may be scheduled; it waits for this grid
+    for (uint32_t g = blockIdx.x * W + warp; 32 * g < SP; g += gridDim.x * W) foi_warp(d, 32 * g, collect_only, koff, sh);
 }
 
 // ------------------------------------------------------------------ infection draws
@@ -1087,28 +1086,34 @@ __device__ __forceinline__ uint32_t batch_instance(const uint32_t* __restrict__ 
     return lo;
 }
 
-// Block-uniform walk over the flattened blocks of a phase. For every block the descriptor of its
-// instance is staged into shared memory (only when the instance changes) and fn(dev, inst, b) runs.
+// Warp runs over the concatenated items of a batch's instances (off[i] = first item of instance
+// i): warps take runs of `run` consecutive items, strided over the grid, so that a warp restages
+// its instance descriptor (per-warp copy in shared memory, wdev) about once per run while every
+// instance is spread over many warps; fn(dev, item within the instance) runs each item.
 template <typename Fn>
-__device__ __forceinline__ void batch_loop(const BatchDev& bd, const uint32_t* __restrict__ off, Fn fn)
+__device__ __forceinline__ void batch_warp_items(const BatchDev& bd, const uint32_t* __restrict__ off, uint32_t run,
+                                                 unsigned long long* wdev, Fn fn)
 {
-    __shared__ __align__(16) unsigned long long raw[sizeof(Dev) / 8];
-    __shared__ uint32_t s_inst;
-    const Dev& d = *reinterpret_cast<const Dev*>(raw);
+    const uint32_t lane = threadIdx.x & 31u, W = blockDim.x >> 5;
+    const Dev& d = *reinterpret_cast<const Dev*>(wdev);
     const uint32_t total = __ldg(&off[bd.n]);
-    uint32_t cur = UINT_MAX;
-    for (uint32_t b = blockIdx.x; b < total; b += gridDim.x) {
-        __syncthreads();  // the previous block's readers of raw / s_inst are done
-        if (threadIdx.x == 0) s_inst = batch_instance(off, bd.n, b);
-        __syncthreads();
-        const uint32_t inst = s_inst;
-        if (inst != cur) {
-            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
-            for (uint32_t i = threadIdx.x; i < sizeof(Dev) / 8; i += blockDim.x) raw[i] = src[i];
-            cur = inst;
-            __syncthreads();
+    const uint32_t runs = (total + run - 1) / run;
+    const uint32_t gw = blockIdx.x * W + (threadIdx.x >> 5), nw = gridDim.x * W;
+    uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its item range
+    for (uint32_t r = gw; r < runs; r += nw) {
+        const uint32_t end = min(total, (r + 1) * run);
+        for (uint32_t it = r * run; it < end; ++it) {
+            if (inst == UINT_MAX || it < lo || it >= hi) {
+                inst = batch_instance(off, bd.n, it);
+                lo = __ldg(&off[inst]);
+                hi = __ldg(&off[inst + 1]);
+                __syncwarp();  // every lane is done with the previous descriptor
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
+                for (uint32_t i = lane; i < sizeof(Dev) / 8; i += 32) wdev[i] = src[i];
+                __syncwarp();
+            }
+            fn(d, it - lo);
         }
-        fn(d, inst, b - __ldg(&off[inst]));
     }
 }
 
@@ -1154,57 +1159,50 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
     griddep_launch_dependents();
 }
 
+// Force-of-infection pass of a batch: one warp per 32 consecutive (serotype, community) pairs of
+// an instance (bd.foi_off counts these warp items), in runs of bd.foi_run items per warp.
 __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
 {
-    __shared__ FoiSmem fs;
+    extern __shared__ __align__(16) unsigned char foi_dyn[];
+    const uint32_t warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    FoiWarpSmem& sh = reinterpret_cast<FoiWarpSmem*>(foi_dyn)[warp];
+    unsigned long long* wdev =
+        reinterpret_cast<unsigned long long*>(foi_dyn + W * sizeof(FoiWarpSmem)) + warp * (sizeof(Dev) / 8);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         griddep_wait();  // the demographic kernel has finished taking items
         *bd.work = 0u;
     }
-    batch_loop(bd, bd.foi_off, [&](const Dev& d, uint32_t, uint32_t b) { foi_block(d, b, 0, koff, fs); });
+    griddep_launch_dependents();  // the infection kernel may be scheduled; it waits for this grid
+    batch_warp_items(bd, bd.foi_off, bd.foi_run, wdev,
+                     [&](const Dev& d, uint32_t item) { foi_warp(d, 32 * item, 0, koff, sh); });
 }
 
 // Infection pass of a batch: one warp per community over the concatenated communities of all
-// instances (bd.infect_off counts communities). Warps take runs of bd.infect_run consecutive
-// communities, strided over the grid, so that a warp restages its instance descriptor (per-warp
-// copy in shared memory, after its tables) about once per run while every instance is spread over
-// many warps.
+// instances (bd.infect_off counts communities), in runs of bd.infect_run communities per warp.
 __global__ void __launch_bounds__(512) k_infect_batch(BatchDev bd, uint32_t koff)
 {
     extern __shared__ __align__(16) unsigned char infect_dyn[];
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, K = blockDim.x >> 5;
+    const uint32_t warp = threadIdx.x >> 5, K = blockDim.x >> 5;
     InfectWarpSmem& sh = reinterpret_cast<InfectWarpSmem*>(infect_dyn)[warp];
     unsigned long long* wdev =
         reinterpret_cast<unsigned long long*>(infect_dyn + K * sizeof(InfectWarpSmem)) + warp * (sizeof(Dev) / 8);
-    const Dev& d = *reinterpret_cast<const Dev*>(wdev);
-    const uint32_t total = __ldg(&bd.infect_off[bd.n]);
-    const uint32_t run = bd.infect_run, runs = (total + run - 1) / run;
-    const uint32_t gw = blockIdx.x * K + warp, nw = gridDim.x * K;
-    uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its community range
-    for (uint32_t r = gw; r < runs; r += nw) {
-        const uint32_t end = min(total, (r + 1) * run);
-        for (uint32_t it = r * run; it < end; ++it) {
-            if (inst == UINT_MAX || it < lo || it >= hi) {
-                inst = batch_instance(bd.infect_off, bd.n, it);
-                lo = __ldg(&bd.infect_off[inst]);
-                hi = __ldg(&bd.infect_off[inst + 1]);
-                __syncwarp();  // every lane is done with the previous descriptor
-                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
-                for (uint32_t i = lane; i < sizeof(Dev) / 8; i += 32) wdev[i] = src[i];
-                __syncwarp();
-            }
-            infect_warp(d, it - lo, koff, sh);
-        }
-    }
+    batch_warp_items(bd, bd.infect_off, bd.infect_run, wdev,
+                     [&](const Dev& d, uint32_t c) { infect_warp(d, c, koff, sh); });
 }
 
-static_assert(16 * (sizeof(InfectWarpSmem) + sizeof(Dev)) <= 48 * 1024,
-              "per-warp infection tables of a 512-thread block must fit the default dynamic shared memory");
+static_assert(16 * (sizeof(InfectWarpSmem) + sizeof(Dev)) <= 48 * 1024 && 16 * (sizeof(FoiWarpSmem) + sizeof(Dev)) <= 48 * 1024,
+              "per-warp tables of a 512-thread block must fit the default dynamic shared memory");
 
 // Dynamic shared memory of the infection kernels for blocks of `threads` threads.
 size_t infect_smem(uint32_t threads, bool batch)
 {
     return (size_t)(threads / 32) * (sizeof(InfectWarpSmem) + (batch ? sizeof(Dev) : 0));
+}
+
+// Dynamic shared memory of the force-of-infection kernels for blocks of `threads` threads.
+size_t foi_smem(uint32_t threads, bool batch)
+{
+    return (size_t)(threads / 32) * (sizeof(FoiWarpSmem) + (batch ? sizeof(Dev) : 0));
 }
 
 __global__ void k_advance_batch(BatchDev bd, uint32_t n)
@@ -1447,8 +1445,9 @@ static int launch_pdl(void (*kernel)(Args...), dim3 grid, dim3 block, size_t sme
 int launch_foi(const Dev& d, const Launch& l, cudaStream_t st, int collect_only, uint32_t koff)
 {
     const uint32_t SP = d.S * d.P;
-    const uint32_t K = l.foiBlock / 4;
-    return launch_pdl(k_foi, dim3(cdiv(SP, K)), dim3(l.foiBlock), 0, st, l.pdl && !collect_only, d, collect_only, koff);
+    const uint32_t pairs = 32 * (l.foiBlock / 32);  // one warp per 32 pairs
+    return launch_pdl(k_foi, dim3(cdiv(SP, pairs)), dim3(l.foiBlock), foi_smem(l.foiBlock, false), st,
+                      l.pdl && !collect_only, d, collect_only, koff);
 }
 
 int launch_infect(const Dev& d, const Launch& l, cudaStream_t st, uint32_t koff)
@@ -1505,7 +1504,9 @@ int batch_blocks_per_sm(const Launch& l, uint32_t out[3])
     else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_demog_batch<1>, (int)l.demogBlock, 0);
     if (e != cudaSuccess) return (int)e;
     out[0] = n > 0 ? (uint32_t)n : 1u;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_foi_batch, (int)l.foiBlock, 0)) != cudaSuccess) return (int)e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_foi_batch, (int)l.foiBlock, foi_smem(l.foiBlock, true))) !=
+        cudaSuccess)
+        return (int)e;
     out[1] = n > 0 ? (uint32_t)n : 1u;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_infect_batch, (int)l.infectBlock,
                                                             infect_smem(l.infectBlock, true))) != cudaSuccess)
@@ -1526,7 +1527,9 @@ int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* e
     else k_demog_batch<1><<<gd, bdm, 0, st>>>(bd, koff);
     if ((e = (int)cudaGetLastError())) return e;
     if (ev) cudaEventRecord(ev[1], st);
-    if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), 0, st, l.pdl != 0, bd, koff))) return e;
+    if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), foi_smem(l.foiBlock, true), st, l.pdl != 0, bd,
+                        koff)))
+        return e;
     if (ev) cudaEventRecord(ev[2], st);
     if ((e = launch_pdl(k_infect_batch, dim3(bd.grid_infect), dim3(l.infectBlock), infect_smem(l.infectBlock, true), st,
                         l.pdl != 0, bd, koff)))

@@ -52,7 +52,7 @@ __host__ __device__ inline int32_t human_next(uint32_t st, int32_t dtime, int32_
 constexpr uint32_t kQuad = 4;  // consecutive recruitment tiles handled by one warp
 constexpr uint32_t kTile = 128;       // mosquito recruitment tile (slots)
 constexpr uint32_t kMaxEventsPerPair = 1u << 24;
-constexpr uint32_t kInfectRunMax = 4;  // most consecutive communities a warp of the batched infection kernel takes
+constexpr uint32_t kInfectRunMax = 4;  // most consecutive items a warp of a batched kernel takes in one run
 
 struct Ctrl {
     uint32_t t;          // current step
@@ -143,11 +143,12 @@ struct BatchDev {
     const uint32_t* demog_off;   // [n+1] demographic warp items (32*U-lane human groups, mosquito quads)
     const uint32_t* demog_h;     // [n] human warp items of each instance (the rest are quads)
     uint32_t* work;              // demographic item counter (zero between steps)
-    const uint32_t* foi_off;     // [n+1] force-of-infection blocks
+    const uint32_t* foi_off;     // [n+1] force-of-infection warp items (32 (serotype, community) pairs each)
     const uint32_t* infect_off;  // [n+1] communities (the infection kernel runs one warp per community)
     uint32_t n;
     uint32_t grid_demog, grid_foi, grid_infect;  // resident CTAs of each persistent kernel
     uint32_t infect_run;                         // consecutive communities per warp run (1..kInfectRunMax)
+    uint32_t foi_run;                            // consecutive force-of-infection items per warp run
 };
 
 struct Launch {
