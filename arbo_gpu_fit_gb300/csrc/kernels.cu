@@ -1031,12 +1031,21 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
                     dt[q] = __ldcg(&d.n_dtime[tg[q]]);
                 }
             }
+            // The group's winning events, then one pass per winner of the lane (the warp runs as
+            // many passes as its busiest lane has winners, not one per event position).
+            uint32_t won = 0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 4; ++q)
+                if (4 * idx + q < k && wk[q] == order_key(hiword, j, 0, 4 * idx + q)) won |= 1u << q;
+            while (won) {
+                const uint32_t q = __ffs(won) - 1;
+                won &= won - 1;
                 const uint32_t e = 4 * idx + q;
-                if (e >= k) break;
-                if (wk[q] == order_key(hiword, j, 0, e))
-                    infect_human(d, tg[q], s, draw4(key, kInfHExposed, ph, t, e), t, im[q], bn[q], dt[q]);
+                const uint32_t tq = q == 0 ? tg[0] : q == 1 ? tg[1] : q == 2 ? tg[2] : tg[3];
+                const uint32_t iq = q == 0 ? im[0] : q == 1 ? im[1] : q == 2 ? im[2] : im[3];
+                const int32_t bq = q == 0 ? bn[0] : q == 1 ? bn[1] : q == 2 ? bn[2] : bn[3];
+                const int32_t dq = q == 0 ? dt[0] : q == 1 ? dt[1] : q == 2 ? dt[2] : dt[3];
+                infect_human(d, tq, s, draw4(key, kInfHExposed, ph, t, e), t, iq, bq, dq);
             }
         } else {
             const uint32_t rel = it - H, j = item_position(sh.mstart, S, rel), idx = rel - sh.mstart[j];
