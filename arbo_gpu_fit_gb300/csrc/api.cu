@@ -1304,8 +1304,9 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     b->blocks[1] = foi_off[n];
     b->blocks[2] = infect_off[n];
     bd.grid_demog = std::max(1u, std::min(b->blocks[0], l.numSM * occ[0]));
-    const uint32_t fwarps = l.numSM * occ[1] * (a.foiBlock / 32);
-    bd.foi_run = std::max(1u, std::min(kInfectRunMax, b->blocks[1] / std::max(fwarps, 1u)));
+    // Force of infection: one item per run. Longer runs left a few warps with the heavy pairs of
+    // large instances (phase 0.29 against 0.12 ms on the 256 large instances; the same on small ones).
+    bd.foi_run = 1;
     bd.grid_foi = std::max(1u, std::min(cdiv(cdiv(b->blocks[1], bd.foi_run), a.foiBlock / 32), l.numSM * occ[1]));
     // Runs of consecutive communities per warp (fewer descriptor restagings), as long as every
     // resident warp still gets one.
