@@ -126,7 +126,7 @@ typedef struct arbo_arch_param {
     uint32_t totalSM;
     uint32_t demogBlock;     /* threads per CTA of the demographic kernel (multiple of 32) */
     uint32_t demogUnroll;    /* 4-agent groups per thread (1, 2 or 4)                      */
-    uint32_t foiBlock;       /* threads per CTA of the force-of-infection kernel           */
+    uint32_t foiBlock;       /* threads per CTA of the force-of-infection kernel (one warp per 32 pairs) */
     uint32_t infectBlock;    /* threads per CTA of the infection kernel (one warp per community) */
     uint32_t graphSteps;     /* steps captured per CUDA graph (0: no graph)                */
     uint32_t demogPipeline;  /* 1: persistent demographic kernel with TMA-staged mosquito tiles
