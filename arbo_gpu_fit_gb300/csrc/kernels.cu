@@ -1279,7 +1279,7 @@ __global__ void k_init_mosquitoes(Dev d)
     if (b >= d.tiles) return;
     const float alive_p = __fdiv_rn(__ldg(&d.etab[0]), (float)d.M);
     const uint32_t c0 = __ldg(&d.tcomm[b]);
-    uint32_t ndead = 0;
+    uint32_t ndead = 0, ndead0 = 0;  // dead slots of the tile; of them, in the tile's first community
     for (int k = 0; k < 4; ++k) {
         const uint32_t i = 4 * (b * 32 + lane) + k;
         if (i >= d.M) {
@@ -1300,7 +1300,9 @@ __global__ void k_init_mosquitoes(Dev d)
             d.m_ple[i] = 0.0f;
             d.m_dtime[i] = INT_MIN;  // never alive: age 0, death age 0
             ndead += 1;
-            atomicSub(&d.mcnt[slot_comm(d, c0, i)], 1u);
+            const uint32_t cc = slot_comm(d, c0, i);
+            if (cc == c0) ndead0 += 1;
+            else atomicSub(&d.mcnt[cc], 1u);
         } else {
             const float randCSF = __fmul_rn(__ldg(&d.survm[d.dm]), u01(r.v[1]));
             const uint32_t a = lower_bound_f(d.survm, d.dm + 1, randCSF);
@@ -1312,8 +1314,14 @@ __global__ void k_init_mosquitoes(Dev d)
             d.m_dtime[i] = death_time(-(int32_t)a, death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f));
         }
     }
+    // One atomic per tile for its first community (a community's alive count would otherwise
+    // take one same-address atomic per dead slot).
     const uint32_t tile_dead = __reduce_add_sync(kFull, ndead);
-    if (lane == 0) d.ledger[b] = (int32_t)tile_dead;
+    const uint32_t dead0 = __reduce_add_sync(kFull, ndead0);
+    if (lane == 0) {
+        d.ledger[b] = (int32_t)tile_dead;
+        if (dead0) atomicSub(&d.mcnt[c0], dead0);
+    }
 }
 
 // nEpidemicInitial / mEpidemicInitial (cpp/epidemicinitial.cu:27-99): the seeded agents are
