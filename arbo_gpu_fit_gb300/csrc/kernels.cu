@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(128, 4) k_demog_tma(Dev d, uint32_t koff)
     griddep_launch_dependents();
 }
 
-// Block b of the demographic pass of one simulation: blocks below hblocks age humans, the others
+// Block b of the demographic pass of one simulation: blocks below hblocks run human groups, the others
 // run one mosquito quad per warp.
 template <int U>
 __device__ __forceinline__ void demog_block(const Dev& d, uint32_t b, uint32_t hblocks, uint32_t koff, QuadSmem* wsm)
