@@ -45,10 +45,11 @@ class IOParamStruct(ctypes.Structure):
 
 class McmcConfigStruct(ctypes.Structure):
     _fields_ = [("chains", c_uint32), ("params", c_uint32), ("replicates", c_uint32), ("months", c_uint32),
-                ("serotypes", c_uint32), ("max_iters", c_uint32), ("report_param", c_uint32), ("reserved", c_uint32),
+                ("serotypes", c_uint32), ("max_iters", c_uint32), ("report_param", c_uint32),
+                ("obs_flags", c_uint32),
                 ("lo", POINTER(ctypes.c_double)), ("hi", POINTER(ctypes.c_double)), ("step", POINTER(ctypes.c_double)),
                 ("observed", POINTER(c_uint32)), ("month_start", POINTER(c_uint32)), ("nb_size", ctypes.c_double),
-                ("seed", c_uint64)]
+                ("seed", c_uint64), ("dispersion_param", c_uint32), ("reserved", c_uint32)]
 
 
 class CSRStruct(ctypes.Structure):
@@ -62,6 +63,9 @@ ARBO_ERR_INVALID, ARBO_ERR_CUDA, ARBO_ERR_ALLOC, ARBO_ERR_DEVICE, ARBO_ERR_STATE
 QUIRK_SEED_RECOVERY_DURATION = 0x1
 QUIRK_SEED_DEAD_MOSQUITO = 0x2
 QUIRKS_REFERENCE = 0x3
+NO_PARAM = 0xFFFFFFFF
+WEEKLY_DAYS, WEEKLY_REFERENCE_FLAT = 0, 1
+OBS_SUM_SEROTYPES, OBS_ZERO_MEAN_FLOOR, OBS_REFERENCE = 0x1, 0x2, 0x3
 DEVERR_EVENT_OVERFLOW = 0x1
 DEVERR_COUNTER = 0x2
 DEVERR_STALL = 0x4
@@ -107,6 +111,7 @@ SIGNATURES = {
     "arbo_sim_launches_per_step": (c_uint32, [c_void_p]),
     "arbo_sim_write_incidence": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
+    "arbo_weekly_from_daily": (c_int, [POINTER(c_uint32), c_uint32, c_uint32, c_uint32, c_int, POINTER(c_uint32)]),
     "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
     "arbo_sim_set_param": (c_int, [c_void_p, POINTER(SimParamStruct)]),
     "arbo_mlp_create": (c_int, [c_uint32, c_uint32, c_uint32, c_uint32, c_uint32, c_uint64, POINTER(c_void_p)]),

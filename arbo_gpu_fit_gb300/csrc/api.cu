@@ -136,6 +136,10 @@ struct arbo_sim {
     size_t flush_bytes = 0;
     std::vector<cudaEvent_t> step_ev;  // per-step event pairs of arbo_sim_time_steps
     uint64_t version = 0;              // bumped when the parameters in d change
+    // Device address of the no-allocation scratch array, looked up by arbo_sim_init on this
+    // handle's device (null when the handle exceeds its size or the lookup failed).
+    unsigned long long* noalloc = nullptr;
+    int noalloc_err = 0;  // cudaError_t of a failed set-up
 };
 
 extern "C" {
@@ -601,6 +605,8 @@ int arbo_sim_set_seed(arbo_sim* s, uint64_t seed, uint32_t instance)
     return ARBO_OK;
 }
 
+static void noalloc_prepare(arbo_sim* s);
+
 int arbo_sim_init(arbo_sim* s, void* stream)
 {
     if (!s) return fail(ARBO_ERR_INVALID, "null handle");
@@ -623,6 +629,7 @@ int arbo_sim_init(arbo_sim* s, void* stream)
     CUDA_TRY(cudaMemcpyAsync(d.mcnt, d.msize, (size_t)d.P * 4, cudaMemcpyDeviceToDevice, st));
     const int e = launch_init(d, s->l, st);
     if (e) return fail(ARBO_ERR_CUDA, std::string("init launch: ") + cudaGetErrorString((cudaError_t)e));
+    noalloc_prepare(s);
     s->host_t = 0;
     s->inited = true;
     return ARBO_OK;
@@ -1117,6 +1124,35 @@ int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, v
     return ARBO_OK;
 }
 
+int arbo_weekly_from_daily(const uint32_t* daily, uint32_t max_time, uint32_t strains, uint32_t max_week, int mode,
+                           uint32_t* out)
+{
+    if ((!daily && max_week) || (!out && max_week) || strains == 0 ||
+        (mode != ARBO_WEEKLY_DAYS && mode != ARBO_WEEKLY_REFERENCE_FLAT))
+        return fail(ARBO_ERR_INVALID, "arbo_weekly_from_daily: bad arguments");
+    const uint64_t rows = (uint64_t)max_time + 1, S = strains;
+    for (uint32_t w = 0; w < max_week; ++w) {
+        uint64_t acc = 0;
+        if (mode == ARBO_WEEKLY_REFERENCE_FLAT) {
+            // cpp/MCMC.cpp:199-210: entry 7w unconditionally, then 7w+k while 7w+k <= maxTime.
+            if (7ull * w >= rows * S)
+                return fail(ARBO_ERR_INVALID, "arbo_weekly_from_daily: week " + std::to_string(w) +
+                                                  " starts past the buffer");
+            acc = daily[7ull * w];
+            for (uint32_t k = 1; k < 7; ++k)
+                if (7ull * w + k <= max_time) acc += daily[7ull * w + k];
+        } else {
+            for (uint32_t k = 0; k < 7; ++k) {
+                const uint64_t t = 7ull * w + k;
+                if (t > max_time) break;
+                for (uint64_t q = 0; q < S; ++q) acc += daily[t * S + q];
+            }
+        }
+        out[w] = (uint32_t)acc;
+    }
+    return ARBO_OK;
+}
+
 int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, void* stream)
 {
     if (!s || !out) return fail(ARBO_ERR_INVALID, "null argument");
@@ -1124,17 +1160,7 @@ int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, voi
     std::vector<uint32_t> inc((size_t)(T + 1) * S);
     int e = arbo_sim_get_series(s, ARBO_SERIES_N_INCIDENCE, inc.data(), inc.size(), stream);
     if (e) return e;
-    // MCMC::storeIncidence (cpp/MCMC.cpp:190-213): week w sums the days 7w..7w+6 that exist.
-    for (uint32_t w = 0; w < max_week; ++w) {
-        uint64_t acc = 0;
-        for (uint32_t k = 0; k < 7; ++k) {
-            const uint64_t t = 7ull * w + k;
-            if (t > T) break;
-            for (uint32_t q = 0; q < S; ++q) acc += inc[t * S + q];
-        }
-        out[w] = (uint32_t)acc;
-    }
-    return ARBO_OK;
+    return arbo_weekly_from_daily(inc.data(), T, S, max_week, ARBO_WEEKLY_DAYS, out);
 }
 
 }  // extern "C"
@@ -1146,28 +1172,30 @@ int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, voi
 // the symbol as an address; it looks the device address up per device.
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[ARBO_NOALLOC_MAX_AGENTS];
 
-namespace {
-std::mutex g_noalloc_mu;
-constexpr int kNoallocMaxDevices = 64;
-unsigned long long* g_noalloc_ptr[kNoallocMaxDevices] = {};
-
-// Device address of the scratch array on `device` (which must be current); looked up once.
-int noalloc_scratch(int device, unsigned long long** out)
+// Set-up of arbo_sim_step_noalloc for handle s, run by arbo_sim_init with s's device current:
+// looks up the scratch array's device address in the context that is current now and loads the
+// step kernels, so that the step call itself neither loads a module (which would commit the
+// array's memory) nor looks anything up. Keeping the address per handle, not per process, means a
+// handle created after a cudaDeviceReset looks it up again in the new context. A failed lookup is
+// recorded for the step call to report, and cleared from the runtime's last error so that it does
+// not surface in an unrelated later call.
+static void noalloc_prepare(arbo_sim* s)
 {
-    if (device < 0 || device >= kNoallocMaxDevices) return fail(ARBO_ERR_INVALID, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(ARBO_ERR_CUDA, std::string("cudaGetSymbolAddress of the no-allocation scratch: ") +
-                                           cudaGetErrorString(e));
-        g_noalloc_ptr[device] = (unsigned long long*)p;
+    s->noalloc = nullptr;
+    s->noalloc_err = 0;
+    const size_t Np = (size_t)s->d.nvec * 4, Mp = (size_t)s->d.tiles * kTile;
+    if (Np + Mp > ARBO_NOALLOC_MAX_AGENTS) return;
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e == cudaSuccess && !p) e = cudaErrorInvalidSymbol;
+    if (e == cudaSuccess) e = (cudaError_t)preload_step_kernels(s->l);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        s->noalloc_err = (int)e;
+        return;
     }
-    *out = g_noalloc_ptr[device];
-    return ARBO_OK;
+    s->noalloc = (unsigned long long*)p;
 }
-}  // namespace
 
 extern "C" int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream)
 {
@@ -1178,10 +1206,12 @@ extern "C" int arbo_sim_step_noalloc(arbo_sim* s, uint32_t nsteps, void* stream)
         return fail(ARBO_ERR_INVALID, "arbo_sim_step_noalloc: " + std::to_string(Np + Mp) +
                                           " padded agents exceed ARBO_NOALLOC_MAX_AGENTS (" +
                                           std::to_string(ARBO_NOALLOC_MAX_AGENTS) + ")");
+    if (!s->noalloc)
+        return fail(ARBO_ERR_CUDA, std::string("arbo_sim_step_noalloc: scratch set-up in arbo_sim_init failed: ") +
+                                       cudaGetErrorString((cudaError_t)s->noalloc_err));
     CUDA_TRY(cudaSetDevice(s->device));
-    unsigned long long* scratch = nullptr;
-    int e = noalloc_scratch(s->device, &scratch);
-    if (e) return e;
+    unsigned long long* scratch = s->noalloc;
+    int e = 0;
     cudaStream_t st = (cudaStream_t)stream;
     const uint32_t n = std::min(nsteps, s->d.T - s->host_t);
     if (n == 0) return ARBO_OK;

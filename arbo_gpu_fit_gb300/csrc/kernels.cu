@@ -1512,6 +1512,24 @@ int launch_advance(const Dev& d, uint32_t n, void* stream)
 
 uint32_t launches_per_step() { return 3; }
 
+int preload_step_kernels(const Launch& l)
+{
+    cudaFuncAttributes a;
+    cudaError_t e;
+    if (l.demogPipeline)
+        e = l.demogUnroll == 4   ? cudaFuncGetAttributes(&a, k_demog_tma<4>)
+            : l.demogUnroll == 2 ? cudaFuncGetAttributes(&a, k_demog_tma<2>)
+                                 : cudaFuncGetAttributes(&a, k_demog_tma<1>);
+    else
+        e = l.demogUnroll == 4   ? cudaFuncGetAttributes(&a, k_demog<4>)
+            : l.demogUnroll == 2 ? cudaFuncGetAttributes(&a, k_demog<2>)
+                                 : cudaFuncGetAttributes(&a, k_demog<1>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_foi);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_infect);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_advance);
+    return (int)e;
+}
+
 int batch_blocks_per_sm(const Launch& l, uint32_t out[3])
 {
     int n = 0;

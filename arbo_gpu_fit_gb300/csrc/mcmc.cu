@@ -24,6 +24,8 @@ namespace {
 struct McmcDev {
     uint32_t C, D, R, Mo, S;  // chains, parameters, replicates per chain, months, serotypes
     uint32_t report;          // index of the reporting-rate parameter
+    uint32_t obs;             // ARBO_OBS_* bits
+    uint32_t disp;            // index of the dispersion parameter (size 1/d), or >= D: nb_size
     double nb_size;
     const double* lo;          // [D]
     const double* hi;          // [D]
@@ -73,11 +75,11 @@ __global__ void k_propose(McmcDev m, uint32_t iter)
 
 // log NB(k; size r, mean mu) = lgamma(k+r) - lgamma(r) - lgamma(k+1) + r log(r/(r+mu)) + k log(mu/(r+mu)),
 // floored at -250 per observation as cpp/MCMC.cpp:238-241 floors it.
-__device__ __forceinline__ double nb_logpmf(uint32_t k, double r, double mu)
+__device__ __forceinline__ double nb_logpmf(uint32_t k, double r, double mu, bool zero_mean_floor)
 {
     double v;
     if (mu <= 0.0) {
-        v = k == 0 ? 0.0 : -INFINITY;
+        v = (k == 0 && !zero_mean_floor) ? 0.0 : -INFINITY;
     } else {
         const double kk = (double)k;
         v = lgamma(kk + r) - lgamma(r) - lgamma(kk + 1.0) - r * log1p(mu / r) + kk * (log(mu) - log(r + mu));
@@ -85,9 +87,10 @@ __device__ __forceinline__ double nb_logpmf(uint32_t k, double r, double mu)
     return fmax(-250.0, v);
 }
 
-// Block (c, r): sum over (month, serotype) cells of the observation log-likelihood of replicate r
-// of chain c (c relative to c0), with mean = reporting rate * simulated monthly cases. Fixed-order
-// double reduction.
+// Block (c, r): sum over (period, serotype) cells of the observation log-likelihood of replicate r
+// of chain c (c relative to c0), with mean = reporting rate * simulated cases of the period (of
+// serotype s, or of all serotypes with sum_s) and size nb_size or 1 / the dispersion parameter
+// (cpp/MCMC.cpp:236-243: NB with r = 1/d, p = d*mu / (1 + d*mu)). Fixed-order double reduction.
 __global__ void __launch_bounds__(256) k_loglik(McmcDev m, const SeriesRef* __restrict__ refs, uint32_t c0, int current)
 {
     __shared__ double part[8];
@@ -95,13 +98,18 @@ __global__ void __launch_bounds__(256) k_loglik(McmcDev m, const SeriesRef* __re
     const SeriesRef ref = refs[cr];
     const double* th = (current ? m.theta : m.prop) + (size_t)c * m.D;
     const double rho = th[m.report];
+    const double size = m.disp < m.D ? 1.0 / th[m.disp] : m.nb_size;
     double acc = 0.0;
     for (uint32_t cell = threadIdx.x; cell < m.Mo * m.S; cell += blockDim.x) {
         const uint32_t mo = cell / m.S, s = cell - mo * m.S;
         uint32_t cases = 0;
-        if (s < ref.S)
+        if (m.obs & ARBO_OBS_SUM_SEROTYPES) {
+            for (uint32_t row = m.mrow[mo]; row < m.mrow[mo + 1] && row <= ref.T; ++row)
+                for (uint32_t q = 0; q < ref.S; ++q) cases += ref.inc[row * ref.S + q];
+        } else if (s < ref.S) {
             for (uint32_t row = m.mrow[mo]; row < m.mrow[mo + 1] && row <= ref.T; ++row) cases += ref.inc[row * ref.S + s];
-        acc += nb_logpmf(m.y[cell], m.nb_size, rho * (double)cases);
+        }
+        acc += nb_logpmf(m.y[cell], size, rho * (double)cases, (m.obs & ARBO_OBS_ZERO_MEAN_FLOOR) != 0);
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31u) == 0) part[threadIdx.x >> 5] = acc;
@@ -204,8 +212,15 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     *out = nullptr;
     const uint32_t C = cfg->chains, D = cfg->params, R = cfg->replicates ? cfg->replicates : 1u;
     if (C == 0 || D == 0 || D > 32 || !cfg->lo || !cfg->hi || !cfg->step || !cfg->observed || !cfg->month_start ||
-        cfg->months == 0 || cfg->serotypes == 0 || cfg->report_param >= D || !(cfg->nb_size > 0.0))
+        cfg->months == 0 || cfg->serotypes == 0 || cfg->report_param >= D || (cfg->obs_flags & ~ARBO_OBS_REFERENCE) ||
+        ((cfg->obs_flags & ARBO_OBS_SUM_SEROTYPES) && cfg->serotypes != 1))
         return mfail(ARBO_ERR_INVALID, "arbo_mcmc_create: bad configuration");
+    if (cfg->dispersion_param == ARBO_NO_PARAM) {
+        if (!(cfg->nb_size > 0.0)) return mfail(ARBO_ERR_INVALID, "arbo_mcmc_create: nb_size must be > 0");
+    } else if (cfg->dispersion_param >= D || cfg->dispersion_param == cfg->report_param ||
+               !(cfg->lo[cfg->dispersion_param] > 0.0)) {
+        return mfail(ARBO_ERR_INVALID, "arbo_mcmc_create: the dispersion parameter needs a box above 0");
+    }
     for (uint32_t mo = 0; mo < cfg->months; ++mo)
         if (cfg->month_start[mo + 1] < cfg->month_start[mo]) return mfail(ARBO_ERR_INVALID, "month_start not ascending");
     arbo_mcmc* h = new arbo_mcmc();
@@ -217,6 +232,8 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     m.Mo = cfg->months;
     m.S = cfg->serotypes;
     m.report = cfg->report_param;
+    m.obs = cfg->obs_flags;
+    m.disp = cfg->dispersion_param == ARBO_NO_PARAM ? D : cfg->dispersion_param;
     m.nb_size = cfg->nb_size;
     m.iters = cfg->max_iters;
     m.k0 = (uint32_t)cfg->seed;

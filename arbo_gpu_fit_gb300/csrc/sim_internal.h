@@ -169,6 +169,10 @@ int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint3
 // Adds n to the step counter and the winner epoch (one thread).
 int launch_advance(const Dev& d, uint32_t n, void* stream);
 uint32_t launches_per_step();
+// Loads the single-instance step kernels for the launch shape of l on the current device (their
+// attributes are queried, which loads a lazily loaded function), so that later launches load no
+// code. Returns the cudaError_t as int.
+int preload_step_kernels(const Launch& l);
 
 // Batched steps (see BatchDev); the block shapes come from l, the grids from bd.
 int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* events, uint32_t koff);

@@ -25,7 +25,7 @@ from typing import Callable, List, Optional
 import numpy as np
 
 from . import configs
-from ._native import McmcConfigStruct, check, load
+from ._native import NO_PARAM, McmcConfigStruct, check, load
 from .simulation import ArchitectureParam, Batch, Simulation
 
 _D = POINTER(ctypes.c_double)
@@ -40,6 +40,14 @@ def month_rows(max_time: int, months: int) -> np.ndarray:
     period m covers steps floor(m*T/months) .. floor((m+1)*T/months) - 1."""
     b = (np.arange(months + 1, dtype=np.int64) * max_time) // months
     return (b + 1).astype(np.uint32)
+
+
+def reference_week_rows(max_time: int, max_week: int) -> np.ndarray:
+    """Period boundaries of the reference's observation model (cpp/MCMC.cpp:199-210, :238): week w
+    covers days 7w..7w+6 of the daily series (rows 7w..7w+6, capped at max_time) and weeks
+    1..max_week-1 are scored (week 0 is skipped). max_week entries: max_week - 1 periods."""
+    b = 7 * np.arange(1, max_week + 1, dtype=np.int64)
+    return np.minimum(b, max_time + 1).astype(np.uint32)
 
 
 def monthly(daily: np.ndarray, rows: np.ndarray) -> np.ndarray:
@@ -74,7 +82,12 @@ class MCMC:
     """Chains of the fit (the reference's MCMC class) with their state on the GPU."""
 
     def __init__(self, workload: configs.Workload, observed: np.ndarray, chains: int, step, seed: int = 1,
-                 replicates: int = 1, max_iters: int = 1000, nb_size: float = 10.0, box=None, report_param: int = 5):
+                 replicates: int = 1, max_iters: int = 1000, nb_size: float = 10.0, box=None, report_param: int = 5,
+                 rows: Optional[np.ndarray] = None, obs_flags: int = 0, dispersion_param: Optional[int] = None):
+        """observed: (periods, series) cases. rows: first daily-series row of each period plus the end
+        (default: equal months over the run). obs_flags (OBS_* of _native) and dispersion_param select
+        the reference's observation model (one series of serotype totals, NB size 1/theta[dispersion_param],
+        zero means scored at the floor) instead of per-serotype series with a fixed size."""
         self._lib = load()
         self.workload = workload
         box = box if box is not None else configs.PRIOR_BOX
@@ -85,12 +98,16 @@ class MCMC:
         self.observed = np.ascontiguousarray(observed, np.uint32)
         self.months = int(self.observed.shape[0])
         self.S = int(self.observed.shape[1])
-        self.rows = month_rows(workload.max_time, self.months)
+        self.rows = np.ascontiguousarray(rows if rows is not None else month_rows(workload.max_time, self.months),
+                                         np.uint32)
+        if self.rows.size != self.months + 1:
+            raise ValueError("rows needs one entry per period plus the end")
         self.max_iters = int(max_iters)
-        cfg = McmcConfigStruct(self.C, self.D, self.R, self.months, self.S, self.max_iters, int(report_param), 0,
-                               _dp(self.lo), _dp(self.hi), _dp(self.step_sd),
+        cfg = McmcConfigStruct(self.C, self.D, self.R, self.months, self.S, self.max_iters, int(report_param),
+                               int(obs_flags), _dp(self.lo), _dp(self.hi), _dp(self.step_sd),
                                self.observed.ctypes.data_as(POINTER(c_uint32)),
-                               self.rows.ctypes.data_as(POINTER(c_uint32)), float(nb_size), int(seed))
+                               self.rows.ctypes.data_as(POINTER(c_uint32)), float(nb_size), int(seed),
+                               NO_PARAM if dispersion_param is None else int(dispersion_param), 0)
         h = c_void_p()
         check(self._lib.arbo_mcmc_create(byref(cfg), byref(h)))
         self._h = h

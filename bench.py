@@ -45,9 +45,9 @@ LAYOUT_BYTES_PER_BIRTH = 14
 FLUSH_MB = 320
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# Per-launch DRAM traffic of the demographic kernel on this workload, from the ncu capture
-# summarised in profiles/k_demog_plain_large.md: dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch (42,423,296 + 7,979,008 bytes).
+# Per-launch DRAM traffic of the demographic kernel on this workload, from one ncu capture of a
+# launch at step 5 (the command is kept with its summary under profiles/):
+# dram__bytes_read.sum + dram__bytes_write.sum (42,423,296 + 7,979,008 bytes).
 DEMOG_TRAFFIC_BYTES = 50_402_304
 
 

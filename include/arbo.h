@@ -331,9 +331,24 @@ uint32_t arbo_sim_launches_per_step(const arbo_sim* s);
  * (writeIncidence, cpp/writeoutput.cpp:13-98) under io->odir. */
 int arbo_sim_write_incidence(arbo_sim* s, uint32_t sim_run, uint32_t mcmc_run, void* stream);
 
-/* Weekly incidence of serotype-summed daily incidence: MCMC::storeIncidence
- * (cpp/MCMC.cpp:190-213) — week w sums days 7w..7w+6 that exist (<= max_time).
- * out has max_week entries. */
+/* Weekly sums of a daily incidence series laid out [t * S + s] for t = 0..max_time, as
+ * MCMC::storeIncidence (cpp/MCMC.cpp:190-213) forms them; out has max_week entries. The reference
+ * walks the flat index 7w + k (k = 0..6, bound 7w + k <= max_time for k >= 1), which is the day
+ * index only when its C_STRAINS is 1, as shipped (cpp/constant.h).
+ *   ARBO_WEEKLY_DAYS: week w sums every serotype of days 7w..7w+6 that exist (<= max_time). For
+ *     S = 1 this equals the reference's arithmetic exactly; for S > 1 it is what the reference
+ *     computes for one serotype applied to the serotype totals, i.e. the fix of the flat indexing
+ *     (which would mix the serotypes of neighbouring days).
+ *   ARBO_WEEKLY_REFERENCE_FLAT: the reference's flat indexing itself, for any S (the entries 7w..7w+6
+ *     of the flat buffer, entry 7w always, the others while 7w + k <= max_time), which is what a
+ *     driver keeping the reference's storeIncidence computes from the same buffer.
+ * Host arithmetic, no device needed. */
+#define ARBO_WEEKLY_DAYS 0
+#define ARBO_WEEKLY_REFERENCE_FLAT 1
+int arbo_weekly_from_daily(const uint32_t* daily, uint32_t max_time, uint32_t strains, uint32_t max_week, int mode,
+                           uint32_t* out);
+/* arbo_weekly_from_daily(ARBO_WEEKLY_DAYS) of the handle's daily incidence series (MCMC::storeIncidence,
+ * cpp/MCMC.cpp:190-213, for a handle of any serotype count). out has max_week entries. */
 int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, void* stream);
 
 /* ------------------------------------------------------------------ stepping without allocation */
@@ -361,8 +376,11 @@ int arbo_sim_weekly_incidence(arbo_sim* s, uint32_t max_week, uint32_t* out, voi
  *    larger handles are rejected with ARBO_ERR_INVALID before anything is launched.
  *  - The scratch array lives in the library's device image, so every GPU that loads the library
  *    holds its 16 MiB until the process exits.
- *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
- *    that device current; make that first call outside any stream capture.
+ *  - Set-up happens in arbo_sim_init, not here: with the handle's device current, init looks up
+ *    the array's device address (cudaGetSymbolAddress) in the current context and loads the step
+ *    kernels, so the module holding the array is loaded, and its memory committed, before the
+ *    first call. Call arbo_sim_init outside any stream capture. The address is kept per handle, so
+ *    a handle created after a cudaDeviceReset looks it up anew.
  *  - All calls, from every handle and thread, share the one array. Each call clears it (a memset on
  *    `stream`) before its first step, so nothing left by an earlier call leaks into the results;
  *    two calls whose work overlaps on the GPU (different streams, no ordering) race on it.
@@ -424,7 +442,7 @@ typedef struct arbo_mcmc_config {
     uint32_t serotypes;    /* observed series per period */
     uint32_t max_iters;    /* chain history kept on the device */
     uint32_t report_param; /* index of the reporting rate: mean cases = rate * simulated cases */
-    uint32_t reserved;
+    uint32_t obs_flags;    /* ARBO_OBS_* bits; 0: observed series s is compared with simulated serotype s */
     const double* lo;      /* [params] prior box (uniform prior) */
     const double* hi;      /* [params] */
     const double* step;    /* [params] random-walk standard deviations */
@@ -433,7 +451,24 @@ typedef struct arbo_mcmc_config {
                                     (row t+1 holds step t), last entry = end */
     double nb_size;        /* negative-binomial size (1 / dispersion of cpp/MCMC.cpp:236) */
     uint64_t seed;
+    uint32_t dispersion_param; /* ARBO_NO_PARAM: the size is nb_size; else the index of the parameter
+                                  holding the dispersion d, size 1/d, fitted like the reference's
+                                  dispersion.candidate (cpp/MCMC.cpp:236-243); its box must be > 0 */
+    uint32_t reserved;
 } arbo_mcmc_config;
+
+#define ARBO_NO_PARAM 0xFFFFFFFFu
+/* Observation-model switches of arbo_mcmc_config.obs_flags. ARBO_OBS_REFERENCE with the weekly
+ * periods of the reference (weeks 1..maxWeek-1, days 7w..7w+6, cpp/MCMC.cpp:199-210 and :238) and a
+ * dispersion parameter is the reference's likelihood, calcEachLogLikelihood (cpp/MCMC.cpp:225-249). */
+#define ARBO_OBS_SUM_SEROTYPES 0x1u  /* a period's simulated cases are summed over every simulated
+                                        serotype and compared with one observed series (serotypes
+                                        must be 1): the reference's totals */
+#define ARBO_OBS_ZERO_MEAN_FLOOR 0x2u /* a cell whose mean is 0 scores the -250 floor whatever its
+                                        count, as cpp/MCMC.cpp:216-221 does (k*log(0) is -inf, or NaN
+                                        for k = 0, and fmax(-250, NaN) is -250); without it a zero
+                                        count at mean 0 scores 0, its exact log-probability */
+#define ARBO_OBS_REFERENCE 0x3u
 
 int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out);
 int arbo_mcmc_destroy(arbo_mcmc* m);

@@ -11,15 +11,23 @@ import os
 import shutil
 import subprocess
 import sys
+import threading
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "liboracle.so"
 FLAGS = ["-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+_lock = threading.Lock()
 
 
 def build_oracle(force: bool = False) -> Path:
+    # Threads of one process build once; processes write their own temporary file and rename it.
+    with _lock:
+        return _build(force)
+
+
+def _build(force: bool) -> Path:
     OUT.mkdir(exist_ok=True)
     h = hashlib.sha256()
     for f in ("oracle.c", "oracle.h"):
@@ -32,7 +40,7 @@ def build_oracle(force: bool = False) -> Path:
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         raise RuntimeError("no C compiler found to build the oracle")
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = LIB.with_suffix(f".so.{os.getpid()}.tmp")
     cmd = [cc, *FLAGS, "-o", str(tmp), str(HERE / "oracle.c"), "-lm"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:

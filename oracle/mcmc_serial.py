@@ -7,6 +7,10 @@ log-likelihood of the observed monthly cases floored at -250 per cell (cpp/MCMC.
 log-mean-exp over replicates (cpp/MCMC.cpp:246-276), and the acceptance test log(u) < logpost' -
 logpost on stream 24 (cpp/MCMC.cpp:278-340). Arithmetic is Python floats (IEEE double) and
 math.lgamma; sums run in cell order, so results agree with the GPU's to rounding, not bit for bit.
+
+``store_incidence``, ``negbinomial_pdf``, ``calc_each_log_likelihood`` and ``calc_log_likelihood``
+restate the reference's own observation model line by line (weekly totals from the flat incidence
+buffer, weeks from 1, fitted dispersion), the checker of the library's ARBO_OBS_REFERENCE mode.
 """
 from __future__ import annotations
 
@@ -51,6 +55,55 @@ def loglik(observed: np.ndarray, dailies, rho: float, rows: np.ndarray, size: fl
         parts.append(acc)
     mx = max(parts)
     return mx + math.log(sum(math.exp(p - mx) for p in parts)) - math.log(len(parts))
+
+
+def store_incidence(flat_daily, max_time: int, max_week: int):
+    """MCMC::storeIncidence (cpp/MCMC.cpp:190-213) as written: week w takes entry 7w of the flat
+    [t * C_STRAINS + s] buffer, then entries 7w+1..7w+6 while 7w+t <= maxTime."""
+    d = [int(x) for x in np.asarray(flat_daily).ravel()]
+    out = []
+    for w in range(max_week):
+        v = d[7 * w]
+        for t in range(1, 7):
+            if w * 7 + t <= max_time:
+                v += d[7 * w + t]
+        out.append(v & 0xFFFFFFFF)
+    return out
+
+
+def negbinomial_pdf(k: int, r: float, p: float) -> float:
+    """negbinomial_pdf (cpp/MCMC.cpp:216-221): lngamma(k+r) - lnfact(k) - lngamma(r) + k log p +
+    r log(1-p), in IEEE double with C's log(0) = -inf and 0 * -inf = NaN."""
+    lp = math.log(p) if p > 0.0 else -math.inf
+    kl = k * lp if not (k == 0 and lp == -math.inf) else math.nan
+    return math.lgamma(k + r) - math.lgamma(k + 1.0) - math.lgamma(r) + kl + r * math.log(1.0 - p)
+
+
+def _fmax(a: float, b: float) -> float:
+    """C fmax: the other argument when one is NaN."""
+    if math.isnan(b):
+        return a
+    if math.isnan(a):
+        return b
+    return max(a, b)
+
+
+def calc_each_log_likelihood(week_sim, data, observation_rate: float, dispersion: float, max_week: int) -> float:
+    """MCMC::calcEachLogLikelihood (cpp/MCMC.cpp:225-249) for one simulation: weeks 1..maxWeek-1,
+    mean = observation rate * simulated weekly incidence, NB with r = 1/dispersion and
+    p = d*mu / (1 + d*mu), each week floored at -250."""
+    ll = 0.0
+    for w in range(1, max_week):
+        mu = observation_rate * float(week_sim[w])
+        p = dispersion * mu / (1.0 + dispersion * mu)
+        ll += _fmax(-250.0, negbinomial_pdf(int(data[w]), 1.0 / dispersion, p))
+    return ll
+
+
+def calc_log_likelihood(particles) -> float:
+    """MCMC::calcLogLikelihood (cpp/MCMC.cpp:252-282): log-mean-exp over the simulations."""
+    mx = max(particles)
+    return mx + math.log(sum(math.exp(p - mx) for p in particles)) - math.log(len(particles))
 
 
 def run(workload, observed, chains, step, seed, iters, theta0, replicates=1, nb_size=10.0, box=None,

@@ -8,10 +8,13 @@ loads the cubins through the CUDA driver API and replays the reference's host la
 reference's include path: ``constant.h`` (four serotypes instead of the shipped one) and
 ``Parameter.h`` (case of cpp/parameter.h). ``ref_layout.cpp`` is compiled against the reference
 headers with the host compiler to record the byte layout of the by-value kernel arguments
-(``layout.json``). The reference's build flags are nvcc defaults, so FMA contraction stays on.
+(``layout.json``). The reference's kernels are compiled with the device flags the reference
+documents for its own build (README.md, "Compilation": ``-O2 -use_fast_math``), so ``powf`` and
+``expf`` in its death tests take the fast approximate forms and FMA contraction stays on.
 
-The reference checkout is read from ``$ARBO_REFERENCE_DIR`` (default ``/root/reference``). Where it
-is absent the prebuilt files in ``oracle/_ref/`` are used as they are.
+The reference checkout is read from ``$ARBO_REFERENCE_DIR``, else from ``REFERENCE_CHECKOUT``, the
+one place this recipe names where the read-only checkout sits on the build machine. Where neither
+exists (the GPU machine) the prebuilt files in ``oracle/_ref/`` are used as they are.
 """
 from __future__ import annotations
 
@@ -31,10 +34,16 @@ REF_SOURCES = ["setuprng", "demographicintial", "epidemicinitial", "ndemographic
                "nepidemic", "mepidemic", "epidemic", "datacollect"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FILES = [f"{n}.cubin" for n in REF_SOURCES] + ["harness.cubin", "layout.json"]
+# Device flags of the reference's documented build (its README, "Compilation").
+REF_FLAGS = ["-O2", "-use_fast_math"]
+
+
+# Where the recipe finds the reference checkout on the build machine when $ARBO_REFERENCE_DIR is unset.
+REFERENCE_CHECKOUT = "/root/reference"
 
 
 def reference_dir() -> Path:
-    return Path(os.environ.get("ARBO_REFERENCE_DIR", "/root/reference"))
+    return Path(os.environ.get("ARBO_REFERENCE_DIR") or REFERENCE_CHECKOUT)
 
 
 def prebuilt() -> bool:
@@ -75,7 +84,7 @@ def build_reference_kernels(force: bool = False) -> Path | None:
     nvcc = _nvcc()
     inc = ["-I", str(SHIM), "-I", str(src), "-include", str(SHIM / "constant.h"), "-include", "cstring",
            "-include", "cmath"]
-    jobs = [[nvcc, "-cubin", *ARCH, "-O3", *inc, str(src / f"{n}.cu"), "-o", str(OUT / f"{n}.cubin")]
+    jobs = [[nvcc, "-cubin", *ARCH, *REF_FLAGS, *inc, str(src / f"{n}.cu"), "-o", str(OUT / f"{n}.cubin")]
             for n in REF_SOURCES]
     jobs.append([nvcc, "-cubin", *ARCH, "-O3", "-lineinfo", str(HERE / "ref_harness.cu"), "-o",
                  str(OUT / "harness.cubin")])
