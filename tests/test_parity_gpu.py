@@ -64,7 +64,10 @@ def test_philox_equals_curand_philox(gpu):
         assert list(out[i]) == ob.philox([i, 0, 0, 0], [seed & 0xFFFFFFFF, seed >> 32])
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=["default", "narrow-nograph", "wide-graph7", "tma-unroll1-graph3"])
+SHAPE_IDS = ["quads-graph64", "narrow-nograph", "wide-graph7", "tma-unroll1-graph3"]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=SHAPE_IDS)
 def test_parity_small_epidemic(gpu, shape):
     w = small_case()
     sim, orc = pair(w, shape)
@@ -73,10 +76,11 @@ def test_parity_small_epidemic(gpu, shape):
 
 
 @pytest.mark.parametrize("quirks", [0, 1, 2])
-def test_parity_quirk_switches(gpu, quirks):
+@pytest.mark.parametrize("pipeline", [0, 1])
+def test_parity_quirk_switches(gpu, quirks, pipeline):
     w = small_case(seed=77, T=25)
     w.parameter.simulation.quirks = quirks
-    sim, orc = pair(w)
+    sim, orc = pair(w, dict(demogPipeline=pipeline))
     run_and_compare(sim, orc, [1, 24])
 
 

@@ -16,16 +16,19 @@ import numpy as np
 import pytest
 
 from arbo_gpu_fit_gb300 import configs
-from arbo_gpu_fit_gb300.simulation import Batch, Simulation
+from arbo_gpu_fit_gb300.simulation import ArchitectureParam, Batch, Parameter, Simulation
 from oracle import binding as ob
 from tests.helpers import compare_state
 
 pytestmark = pytest.mark.gpu
 
 
-def test_parity_plain_large_workload(gpu):
+@pytest.mark.parametrize("pipeline", [0, 1], ids=["quads", "tma-quads"])
+def test_parity_plain_large_workload(gpu, pipeline):
     w = configs.plain_large()
-    sim = Simulation(w.parameter, w.network, w.n_sizes, w.m_sizes, max_time=w.max_time, seed=w.seed)
+    arch = ArchitectureParam(0, demogPipeline=pipeline)
+    sim = Simulation(Parameter(w.parameter.simulation, arch), w.network, w.n_sizes, w.m_sizes, max_time=w.max_time,
+                     seed=w.seed)
     orc = ob.OracleSim(w.parameter.simulation, w.network, w.n_sizes, w.m_sizes, w.max_time, w.seed)
     try:
         sim.init()
