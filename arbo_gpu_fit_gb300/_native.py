@@ -52,6 +52,14 @@ class McmcConfigStruct(ctypes.Structure):
                 ("seed", c_uint64), ("dispersion_param", c_uint32), ("reserved", c_uint32)]
 
 
+class CensusExportStruct(ctypes.Structure):
+    """arbo_census_export: device pointers of the reference's census buffers (NULL: skipped)."""
+    _fields_ = [(n, c_void_p) for n in (
+        "n_age", "n_exposed", "n_history", "n_infect_status", "n_ple", "n_recovery", "n_strain", "n_sub_population",
+        "n_sub_pop_index", "m_age", "m_dead", "m_exposed", "m_infect_status", "m_ple", "m_strain", "m_sub_population",
+        "m_sub_pop_index")]
+
+
 class CSRStruct(ctypes.Structure):
     _fields_ = [("subPopTotal", c_uint32), ("nnz", c_uint32), ("loc", POINTER(c_uint32)), ("to", POINTER(c_uint32)),
                 ("weight", POINTER(c_float))]
@@ -111,6 +119,7 @@ SIGNATURES = {
     "arbo_sim_launches_per_step": (c_uint32, [c_void_p]),
     "arbo_sim_write_incidence": (c_int, [c_void_p, c_uint32, c_uint32, c_void_p]),
     "arbo_sim_weekly_incidence": (c_int, [c_void_p, c_uint32, POINTER(c_uint32), c_void_p]),
+    "arbo_sim_export_census": (c_int, [c_void_p, POINTER(CensusExportStruct), c_void_p]),
     "arbo_weekly_from_daily": (c_int, [POINTER(c_uint32), c_uint32, c_uint32, c_uint32, c_int, POINTER(c_uint32)]),
     "arbo_sim_step_noalloc": (c_int, [c_void_p, c_uint32, c_void_p]),
     "arbo_sim_set_param": (c_int, [c_void_p, POINTER(SimParamStruct)]),

@@ -872,6 +872,16 @@ int arbo_sim_get_census(arbo_sim* s, arbo_census_field f, void* host, size_t byt
     return ARBO_OK;
 }
 
+int arbo_sim_export_census(arbo_sim* s, const arbo_census_export* out, void* stream)
+{
+    if (!s || !out) return fail(ARBO_ERR_INVALID, "null argument");
+    if (!s->inited) return fail(ARBO_ERR_STATE, "arbo_sim_export_census before arbo_sim_init");
+    CUDA_TRY(cudaSetDevice(s->device));
+    const int e = launch_export(s->d, *out, stream);
+    if (e) return fail(ARBO_ERR_CUDA, std::string("census export: ") + cudaGetErrorString((cudaError_t)e));
+    return ARBO_OK;
+}
+
 // Recomputes every human's next event time from its status, times and ages (after a census write
 // that changed any of them).
 static int refresh_human_next(arbo_sim* s, void* stream)

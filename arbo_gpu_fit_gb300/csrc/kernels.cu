@@ -1388,7 +1388,57 @@ __global__ void k_advance(Dev d, uint32_t n)
     }
 }
 
+// Census export in the reference's types (arbo_sim_export_census): one thread per agent.
+__global__ void k_export_humans(Dev d, arbo_census_export x)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const int32_t now = (int32_t)d.ctrl->t;
+    if (x.n_age) x.n_age[i] = (uint16_t)(now - d.n_born[i]);
+    if (x.n_exposed) x.n_exposed[i] = (uint16_t)d.n_exposed[i];
+    if (x.n_recovery) x.n_recovery[i] = (uint16_t)d.n_recovery[i];
+    if (x.n_infect_status) x.n_infect_status[i] = d.n_status[i];
+    if (x.n_ple) x.n_ple[i] = d.n_ple[i];
+    if (x.n_strain) x.n_strain[i] = d.n_strain[i];
+    if (x.n_sub_population) x.n_sub_population[i] = human_comm(d.nloc, d.hcomm, d.P, i);
+    if (x.n_sub_pop_index) x.n_sub_pop_index[i] = i;
+    if (x.n_history) {
+        const uint32_t imm = d.n_imm[i];
+        for (uint32_t s = 0; s < d.S; ++s) x.n_history[(size_t)s * d.N + i] = ((imm >> s) & 1u) ? -2 : -1;
+    }
+}
+
+__global__ void k_export_mosquitoes(Dev d, arbo_census_export x)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.M) return;
+    const int32_t now = (int32_t)d.ctrl->t;
+    const uint32_t st = d.m_state[i];
+    if (x.m_age) {
+        // Alive: steps since birth; dead: the age it died at (0 for a slot dead since initialisation).
+        const int32_t b = d.m_born[i], dt = d.m_dtime[i];
+        int32_t a = now - b;
+        if (st & kDead) a = dt == INT_MIN ? 0 : max(dt, max(b, 0) + 1) - b;
+        x.m_age[i] = (uint16_t)a;
+    }
+    if (x.m_dead) x.m_dead[i] = (st & kDead) ? 1 : 0;
+    if (x.m_exposed) x.m_exposed[i] = (uint16_t)d.m_exposed[i];
+    if (x.m_infect_status) x.m_infect_status[i] = (uint8_t)(st & 3u);
+    if (x.m_ple) x.m_ple[i] = d.m_ple[i];
+    if (x.m_strain) x.m_strain[i] = d.m_strain[i];
+    if (x.m_sub_population) x.m_sub_population[i] = slot_comm(d, __ldg(&d.tcomm[i / kTile]), i);
+    if (x.m_sub_pop_index) x.m_sub_pop_index[i] = i;
+}
+
 }  // namespace
+
+int launch_export(const Dev& d, const arbo_census_export& x, void* stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (d.N) k_export_humans<<<cdiv(d.N, 256), 256, 0, st>>>(d, x);
+    if (d.M) k_export_mosquitoes<<<cdiv(d.M, 256), 256, 0, st>>>(d, x);
+    return (int)cudaGetLastError();
+}
 
 int launch_l2_flush(const void* buf, size_t bytes, uint32_t* sink, uint32_t num_sm, cudaStream_t st)
 {

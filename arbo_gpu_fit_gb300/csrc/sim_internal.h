@@ -22,9 +22,8 @@
 #include <climits>
 #include <string>
 
+#include "../../include/arbo.h"
 #include "philox.cuh"
-
-struct arbo_sim;  // include/arbo.h
 
 namespace arbo {
 
@@ -168,6 +167,8 @@ int demog_tma_blocks_per_sm(uint32_t unroll);
 int launch_step(const Dev& d, const Launch& l, void* stream, void* events, uint32_t koff);
 // Adds n to the step counter and the winner epoch (one thread).
 int launch_advance(const Dev& d, uint32_t n, void* stream);
+// Writes the census in the reference's types into the caller's buffers (arbo_sim_export_census).
+int launch_export(const Dev& d, const arbo_census_export& x, void* stream);
 uint32_t launches_per_step();
 // Loads the single-instance step kernels for the launch shape of l on the current device (their
 // attributes are queried, which loads a lazily loaded function), so that later launches load no

@@ -25,6 +25,10 @@ THETA_TRUE = np.array([0.5, 0.5, 0.9, 0.5, 100.0, 0.1])
 # burn-in): the posterior is narrow, a step of 1 % of the box already lowers the log-likelihood by
 # about 5 at the true vector on both populations, with a seed-to-seed spread of 2-4.
 STEP_FRACTION = 0.01
+# Acceptance rate the burn-in adaptation aims at (a one-element list so the command line can set it).
+# Pseudo-marginal chains, whose likelihood is a noisy estimate, do best well below the 0.234 of
+# exact random-walk Metropolis (Sherlock et al. 2015 give about 0.07 at the optimal noise level).
+TARGET_ACCEPT = [0.234]
 
 
 @dataclass
@@ -65,18 +69,21 @@ def setup(population: str = "small", chains: int = 64, months: int = 120, seed: 
 
 
 def summarize(chain: np.ndarray, minutes: float, burn: int) -> dict:
-    """Posterior summary of recorded states [iters, chains, D] after discarding `burn` iterations."""
+    """Posterior summary of recorded states [iters, chains, D] after discarding `burn` iterations:
+    multi-chain ESS and split R-hat per parameter, ESS per minute, posterior means."""
     k = int(burn)
     post = chain[k:]
     e = mcmc.ess(post)
+    r = mcmc.rhat(post)
     return {"iters": int(chain.shape[0]), "kept": int(post.shape[0]), "ess": e.tolist(), "ess_min": float(e.min()),
+            "rhat": r.tolist(), "rhat_max": float(np.nanmax(r)) if np.isfinite(r).any() else None,
             "minutes": minutes, "ess_per_min": float(e.min() / minutes) if minutes > 0 else None,
             "mean": post.reshape(-1, post.shape[2]).mean(0).tolist()}
 
 
 def run_plain(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
-    r = mcmc.run_plain(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
+    r = mcmc.run_plain(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]))
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
     out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
@@ -100,11 +107,12 @@ def train_surrogate(fs: FitSetup, runs: int, epochs: int, seed: int = 3, hidden:
 def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
     r = mcmc.run_delayed(m, iters, fs.theta0, lambda th: sur.loglik(th, fs.observed),
-                         adapt=mcmc.StepAdapter(adapt_until))
+                         adapt=mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]))
     chain, flags = m.chain(iters)
+    accept_per_iter = flags[1:].mean()
     st = m.state()
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
-    out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
+    out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(accept_per_iter),
                passed=float(st["passed"].sum() / (fs.chains * (iters - 1))), s_per_iter=r["wall_s"] / iters,
                chain=chain)
     m.close()
@@ -113,44 +121,60 @@ def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_u
 
 def run_batched(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
-    r = mcmc.run_batched(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until))
+    adapt = mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0])
+    r = mcmc.run_batched(m, iters, fs.theta0, adapt=adapt)
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
     out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
-               s_per_iter=r["wall_s"] / iters, chain=chain)
+               s_per_iter=r["wall_s"] / iters, chain=chain, flags=flags, schedule=adapt.schedule(fs.step, iters),
+               mcmc_seed=seed)
     m.close()
     return out
 
 
 def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt_until: int = 60,
             plain_iters: int = 20, train_runs: int = 4096, epochs: int = 60, seed: int = 11,
-            step_fraction: float = STEP_FRACTION, replicates: int = 1) -> dict:
+            step_fraction: float = STEP_FRACTION, replicates: int = 1, start: str = "near",
+            save: str | None = None) -> dict:
     """Plain, batched and batched + surrogate (delayed acceptance) chains on one setup.
 
     Plain and batched produce bit-identical chains (the random streams are keyed; tested), so the
     plain chain's effective sample size for `iters` iterations is the batched chain's, and its
     time is plain_iters measured iterations scaled to `iters` (every iteration simulates every
     chain once). The first plain_iters states of both are compared here as well."""
-    fs = setup(population, chains=chains, seed=seed, step_fraction=step_fraction, replicates=replicates)
-    out = {"population": population, "step_fraction": step_fraction, "replicates": replicates, "chains": chains, "iters": iters, "adapt_until": adapt_until,
-           "theta_true": THETA_TRUE.tolist()}
+    fs = setup(population, chains=chains, seed=seed, step_fraction=step_fraction, replicates=replicates, start=start)
+    out = {"population": population, "start": start, "target_accept": TARGET_ACCEPT[0],
+           "step_fraction": step_fraction, "replicates": replicates,
+           "chains": chains, "iters": iters, "adapt_until": adapt_until, "theta_true": THETA_TRUE.tolist()}
     b = run_batched(fs, iters, adapt_until=adapt_until)
     p = run_plain(fs, plain_iters, adapt_until=adapt_until)
     same = bool(np.array_equal(p["chain"], b["chain"][:plain_iters]))
     plain_minutes = p["s_per_iter"] * iters / 60.0
     plain = {"s_per_iter": p["s_per_iter"], "measured_iters": plain_iters, "minutes_for_iters": plain_minutes,
-             "ess_min": b["ess_min"], "ess_per_min": b["ess_min"] / plain_minutes, "same_chain_as_batched": same}
+             "ess_min": b["ess_min"], "ess_per_min": b["ess_min"] / plain_minutes if plain_minutes > 0 else None,
+             "same_chain_as_batched": same}
     sur, info = train_surrogate(fs, train_runs, epochs, seed=seed)
     d = run_delayed(fs, sur, iters, adapt_until=adapt_until)
     train_min = (info["simulate_s"] + info["train_s"]) / 60.0
+    if save:
+        np.savez_compressed(save, population=population, seed=seed, replicates=replicates, chains=chains,
+                            months=fs.months, theta0=fs.theta0, observed=fs.observed, step0=fs.step,
+                            schedule=b["schedule"], mcmc_seed=b["mcmc_seed"], batched_chain=b["chain"],
+                            batched_flags=b["flags"], delayed_chain=d["chain"], adapt_until=adapt_until)
     for r_ in (b, d):
         r_.pop("chain")
+    for k_ in ("flags", "schedule"):
+        b.pop(k_)
     p.pop("chain")
     out.update(plain=plain, batched=b, delayed=d, surrogate=info)
+    def ratio(a, b):
+        return a / b if a is not None and b else None
+
     out["delayed"]["ess_per_min_incl_training"] = d["ess_min"] / (d["minutes"] + train_min)
-    out["speedup_batched_vs_plain"] = b["ess_per_min"] / plain["ess_per_min"]
-    out["speedup_delayed_vs_plain"] = d["ess_per_min"] / plain["ess_per_min"]
-    out["speedup_delayed_vs_plain_incl_training"] = out["delayed"]["ess_per_min_incl_training"] / plain["ess_per_min"]
+    out["speedup_batched_vs_plain"] = ratio(b["ess_per_min"], plain["ess_per_min"])
+    out["speedup_delayed_vs_plain"] = ratio(d["ess_per_min"], plain["ess_per_min"])
+    out["speedup_delayed_vs_plain_incl_training"] = ratio(out["delayed"]["ess_per_min_incl_training"],
+                                                          plain["ess_per_min"])
     mb, md = np.array(b["mean"]), np.array(d["mean"])
     out["delayed_mean_rel_diff_vs_exact"] = (np.abs(md - mb) / np.abs(mb)).tolist()
     return out
@@ -203,18 +227,23 @@ def main(argv=None):
     ap.add_argument("--replicates", type=int, default=1, help="simulations per proposal (log-mean-exp)")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--target-accept", type=float, default=0.234, help="acceptance aimed at during burn-in")
+    ap.add_argument("--start", choices=["near", "spread"], default="near",
+                    help="chains start near the true vector or over the middle half of the box")
+    ap.add_argument("--save", default=None, help="npz with the chains, data and step schedule (for a serial check)")
     ap.add_argument("--time-batch", type=int, default=0, help="time one batch of this many handles and exit")
     ap.add_argument("--time-steps", type=int, default=2)
     ap.add_argument("--warm-steps", type=int, default=160)
     a = ap.parse_args(argv)
     _native.check(_native.load().arbo_set_device(a.device))
+    TARGET_ACCEPT[0] = a.target_accept
     if a.time_batch:
         print(json.dumps(time_batch(a.population, a.time_batch, a.time_steps, a.warm_steps)))
         return
     t0 = time.perf_counter()
     r = compare(a.population, chains=a.chains, iters=a.iters, adapt_until=a.adapt, plain_iters=a.plain_iters,
                 train_runs=a.train_runs, epochs=a.epochs, step_fraction=a.step_fraction,
-                replicates=a.replicates)
+                replicates=a.replicates, start=a.start, save=a.save)
     r["total_s"] = time.perf_counter() - t0
     text = json.dumps(r, indent=1)
     if a.out:

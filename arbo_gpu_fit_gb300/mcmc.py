@@ -220,6 +220,7 @@ class StepAdapter:
         self.until, self.every, self.target = int(until), int(every), float(target)
         self.last = None
         self.history = []
+        self.steps = {}  # iteration -> standard deviations in force from that iteration on
 
     def __call__(self, m: "MCMC", it: int) -> None:
         if it > self.until or it % self.every:
@@ -230,7 +231,17 @@ class StepAdapter:
             f = float(np.clip(np.exp(2.0 * (rate - self.target)), 0.5, 2.0))
             m.set_step(m.step_sd * f)
             self.history.append((it, rate, f))
+            self.steps[it + 1] = m.step_sd.copy()
         self.last = acc
+
+    def schedule(self, step0: np.ndarray, iters: int) -> np.ndarray:
+        """Standard deviations used by the proposal of every iteration, [iters, D]."""
+        out = np.zeros((iters, len(step0)))
+        cur = np.asarray(step0, np.float64)
+        for it in range(iters):
+            cur = self.steps.get(it, cur)
+            out[it] = cur
+        return out
 
 
 def _simulate_alone(sim: Simulation):
@@ -404,6 +415,22 @@ def ess(samples: np.ndarray) -> np.ndarray:
             tau += 2 * pair
         out[d] = m2 * n / max(tau, 1e-12)
     return out
+
+
+def rhat(samples: np.ndarray) -> np.ndarray:
+    """Split-chain potential scale reduction per parameter (Gelman et al., BDA3 11.4): every chain is
+    split in halves, and R-hat = sqrt(((n-1)/n W + B/n) / W) over the 2m half-chains of length n.
+    samples: (iters, chains, D). Values near 1 (< 1.1) mean the chains agree."""
+    n_all, _, D = samples.shape
+    half = n_all // 2
+    if half < 2:
+        return np.full(D, np.nan)
+    x = np.concatenate([samples[:half], samples[half:2 * half]], axis=1)
+    n = x.shape[0]
+    W = x.var(axis=0, ddof=1).mean(axis=0)
+    B = n * x.mean(axis=0).var(axis=0, ddof=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.sqrt(((n - 1) / n * W + B / n) / W)
 
 
 # -- output files in the reference's formats (cpp/MCMC.cpp:383-484) --------------------------------

@@ -302,6 +302,38 @@ int arbo_sim_get_counters(arbo_sim* s, arbo_counter_kind kind, void* host, size_
  * computed on the copy (at the current step; a dead mosquito slot reads the age at which it
  * died) and cannot be set (ARBO_ERR_INVALID). */
 int arbo_sim_get_census(arbo_sim* s, arbo_census_field field, void* host, size_t bytes, void* stream);
+
+/* The census in the reference's own types and layouts (cpp/censustypedef.h:8-16), as the census
+ * buffers of simulation() (cpp/simulation.h:16-30) hold it after a run: device pointers on the
+ * handle's device, any of them NULL to skip that field. Ages, exposed and recovery ages are uint16
+ * (the reference's age type, which wraps above 65535 days); history is [serotype * N + human] with
+ * -1 for a serotype the human is naive to and -2 for one it is immune to (the reference's marker of
+ * immunity without a recorded age, cpp/demographicintial.cu:164; this library keeps the immunity,
+ * not the age at infection); sub-population indices are the community-sorted order, i.e. the
+ * identity. A dead mosquito slot reads the age it died at, as arbo_sim_get_census gives it. */
+typedef struct arbo_census_export {
+    uint16_t* n_age;            /* [N] */
+    uint16_t* n_exposed;        /* [N] */
+    int32_t* n_history;         /* [S * N] */
+    uint8_t* n_infect_status;   /* [N] */
+    float* n_ple;               /* [N] */
+    uint16_t* n_recovery;       /* [N] */
+    uint8_t* n_strain;          /* [N] */
+    uint32_t* n_sub_population; /* [N] community of each human */
+    uint32_t* n_sub_pop_index;  /* [N] census indices sorted by community */
+    uint16_t* m_age;            /* [M] */
+    uint8_t* m_dead;            /* [M] */
+    uint16_t* m_exposed;        /* [M] */
+    uint8_t* m_infect_status;   /* [M] */
+    float* m_ple;               /* [M] */
+    uint8_t* m_strain;          /* [M] */
+    uint32_t* m_sub_population; /* [M] */
+    uint32_t* m_sub_pop_index;  /* [M] */
+} arbo_census_export;
+
+/* Writes the handle's census into the caller's device buffers of `out` (stream-ordered, no host
+ * copy): the census half of the outputs of simulation() (cpp/simulation.h:16-30). */
+int arbo_sim_export_census(arbo_sim* s, const arbo_census_export* out, void* stream);
 int arbo_sim_set_census(arbo_sim* s, arbo_census_field field, const void* host, size_t bytes, void* stream);
 int arbo_sim_set_counters(arbo_sim* s, arbo_counter_kind kind, const void* host, size_t n, void* stream);
 

@@ -16,12 +16,17 @@
  *   counters d_nInfectedSubPopCount, d_mInfectedSubPopCount, d_nIncidenceSubPop [S*P],
  *            d_nSubPopCount, d_mSubPopCount, d_nSubPopLoc, d_mSubPopLoc, d_nSubPopSize,
  *            d_mSubPopSize [P] (state at the end of the run);
+ *   census   d_nAge, d_nExposed, d_nHistory [S*N], d_nInfectStatus, d_nPLE, d_nRecovery, d_nStrain,
+ *            d_nSubPopulation, d_nSubPopIndex [N]; d_mAge, d_mDead, d_mExposed, d_mInfectStatus,
+ *            d_mPLE, d_mStrain, d_mSubPopulation, d_mSubPopIndex [M] (end of the run, by
+ *            arbo_sim_export_census on the device: history -1 naive / -2 immune, since the library
+ *            keeps immunity but not the age at infection; the index is the community-sorted order);
  *   file     nData<h_mcmcRun>.csv under h_parameter.io.get_odir(), as writeIncidence
  *            (cpp/writeoutput.cpp:13-98) appends it at the end of the reference's simulation().
- * so that MCMC::storeIncidence (cpp/MCMC.cpp:190-213) reads d_nIncidence as before. The
- * library keeps its own census (birth and death times instead of ages, community-sorted), so the
- * census, RNG-state, index, reduction and age-of-infection buffers of the signature are left
- * untouched; arbo_sim_get_census reads the census in the reference's fields.
+ * so that MCMC::storeIncidence (cpp/MCMC.cpp:190-213) reads d_nIncidence as before and a driver
+ * that writes the census out afterwards (cpp/writeoutput.cpp:101-241) reads the final census. The
+ * RNG-state, reduction, survival, dead-count and age-of-infection buffers of the signature are the
+ * reference's scratch and are left untouched.
  *
  * Differences from the reference's call:
  *   - the network is the caller's CSR (d_sparseNet*), community sizes are the caller's
@@ -158,10 +163,11 @@ inline void simulation(age* d_nAge, exposed* d_nExposed, history* d_nHistory, in
                        const uint32_t h_subPopTotal, const ClimateData h_climateData, const uint32_t h_simRun,
                        const uint32_t h_mcmcRun, const uint32_t maxTime)
 {
-    (void)d_nAge, (void)d_nExposed, (void)d_nHistory, (void)d_nInfectStatus, (void)d_nPLE, (void)d_nRecovery;
-    (void)d_nStrain, (void)d_nSubPopulation, (void)d_mAge, (void)d_mDead, (void)d_mExposed, (void)d_mInfectStatus;
-    (void)d_mPLE, (void)d_mStrain, (void)d_mSubPopulation, (void)d_randStates, (void)d_nSubPopIndex;
-    (void)d_mSubPopIndex, (void)d_nTransmission, (void)d_mTransmission, (void)d_nAgeOfInfection;
+    static_assert(sizeof(age) == 2 && sizeof(exposed) == 2 && sizeof(recovery) == 2 && sizeof(history) == 4 &&
+                      sizeof(infectStatus) == 1 && sizeof(dead) == 1 && sizeof(strain) == 1 &&
+                      sizeof(pLifeExpectancy) == 4 && sizeof(subPopulation) == 4,
+                  "the census types of cpp/censustypedef.h");
+    (void)d_randStates, (void)d_nTransmission, (void)d_mTransmission, (void)d_nAgeOfInfection;
     (void)d_nAgeOfInfectionCount, (void)d_mDeadCount, (void)d_nSurvival, (void)d_mSurvival;
     (void)d_nReductionInfectedCount, (void)d_nReductionCount, (void)d_mReductionCount, (void)d_nSize, (void)d_mSize;
     (void)d_subPopTotal, (void)d_mExpectedPopSize, (void)nGridSize, (void)mGridSize, (void)h_climateData;
@@ -268,6 +274,16 @@ inline void simulation(age* d_nAge, exposed* d_nExposed, history* d_nHistory, in
                     deliver(d_mSubPopLoc, P, counter(ARBO_COUNTER_M_SUBPOP_LOC, (size_t)P + 1)) &&
                     deliver(d_nSubPopSize, P, copy_sizes(nsize)) && deliver(d_mSubPopSize, P, copy_sizes(msize));
     if (!ok) return (void)report(ARBO_ERR_CUDA, "outputs");
+    arbo_census_export cx = {reinterpret_cast<uint16_t*>(d_nAge), reinterpret_cast<uint16_t*>(d_nExposed),
+                             reinterpret_cast<int32_t*>(d_nHistory), reinterpret_cast<uint8_t*>(d_nInfectStatus),
+                             reinterpret_cast<float*>(d_nPLE), reinterpret_cast<uint16_t*>(d_nRecovery),
+                             reinterpret_cast<uint8_t*>(d_nStrain), reinterpret_cast<uint32_t*>(d_nSubPopulation),
+                             d_nSubPopIndex, reinterpret_cast<uint16_t*>(d_mAge), reinterpret_cast<uint8_t*>(d_mDead),
+                             reinterpret_cast<uint16_t*>(d_mExposed), reinterpret_cast<uint8_t*>(d_mInfectStatus),
+                             reinterpret_cast<float*>(d_mPLE), reinterpret_cast<uint8_t*>(d_mStrain),
+                             reinterpret_cast<uint32_t*>(d_mSubPopulation), d_mSubPopIndex};
+    if (!report(arbo_sim_export_census(s.sim, &cx, nullptr), "census") || cudaDeviceSynchronize() != cudaSuccess)
+        return (void)report(ARBO_ERR_CUDA, "census");
     report(arbo_sim_write_incidence(s.sim, h_simRun, h_mcmcRun, nullptr), "nData output");
 }
 

@@ -107,8 +107,14 @@ def calc_log_likelihood(particles) -> float:
 
 
 def run(workload, observed, chains, step, seed, iters, theta0, replicates=1, nb_size=10.0, box=None,
-        report_param=5):
-    """Returns (chain[iters, chains, D], accepted flags[iters, chains], logpost[chains])."""
+        report_param=5, subset=None, threads=1):
+    """Returns (chain[iters, n, D], accepted flags[iters, n], logpost[n]) for the chains in `subset`
+    (default: all), n = len(subset). `step` is one vector of random-walk standard deviations or a
+    schedule [iters, D] (the burn-in adaptation of a GPU run); theta0 holds every chain's start.
+    `threads` > 1 runs the oracle simulations of an iteration in parallel threads (the oracle is C
+    code called through ctypes, which releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
     box = box if box is not None else configs.PRIOR_BOX
     lo = np.array([b[1] for b in box])
     hi = np.array([b[2] for b in box])
@@ -116,42 +122,60 @@ def run(workload, observed, chains, step, seed, iters, theta0, replicates=1, nb_
     key = [seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF]
     rows = month_rows(workload.max_time, observed.shape[0])
     w = workload
+    subset = list(range(chains)) if subset is None else [int(c) for c in subset]
+    steps = np.asarray(step, np.float64)
+    if steps.ndim == 1:
+        steps = np.repeat(steps[None], iters, axis=0)
 
-    def simulate(theta, c, r, it):
+    def simulate(args):
+        theta, c, r, it = args
         sp = configs.apply_theta(w.parameter.simulation, np.clip(theta, lo, hi))
         orc = ob.OracleSim(sp, w.network, w.n_sizes, w.m_sizes, w.max_time, sim_seed(w.seed, c, r, it))
-        orc.init()
-        orc.step(w.max_time)
-        return orc.series("n_incidence")
+        try:
+            orc.init()
+            orc.step(w.max_time)
+            return orc.series("n_incidence")
+        finally:
+            orc.close()
 
     def inbox(th):
         return bool(np.all((th >= lo) & (th <= hi)))
 
-    theta = np.array(theta0, np.float64).reshape(chains, D).copy()
-    logpost = np.zeros(chains)
-    out = np.zeros((iters, chains, D))
-    flags = np.zeros((iters, chains), bool)
-    for c in range(chains):
-        ll = loglik(observed, [simulate(theta[c], c, r, 0) for r in range(replicates)], theta[c][report_param], rows,
-                    nb_size)
-        logpost[c] = ll if inbox(theta[c]) else -math.inf
-    out[0] = theta
-    flags[0] = True
-    for it in range(1, iters):
-        for c in range(chains):
-            prop = theta[c].copy()
-            for d in range(D):
-                v = _draw(key, STREAM_PROPOSE, c, it, d)
-                z = math.sqrt(-2.0 * math.log(u01d(v[0], v[1]))) * math.cos(6.283185307179586 * u01d(v[2], v[3]))
-                prop[d] = theta[c][d] + step[d] * z
-            ll = loglik(observed, [simulate(prop, c, r, it) for r in range(replicates)], prop[report_param], rows,
-                        nb_size)
-            lp = ll if inbox(prop) else -math.inf
-            v = _draw(key, STREAM_ACCEPT, c, it)
-            acc = lp > -math.inf and math.log(u01d(v[0], v[1])) < lp - logpost[c]
-            if acc:
-                theta[c] = prop
-                logpost[c] = lp
-            out[it, c] = theta[c]
-            flags[it, c] = acc
+    pool = ThreadPoolExecutor(max_workers=max(1, int(threads)))
+
+    def logliks(thetas, it):
+        jobs = [(thetas[j], c, r, it) for j, c in enumerate(subset) for r in range(replicates)]
+        series = list(pool.map(simulate, jobs))
+        return [loglik(observed, series[j * replicates:(j + 1) * replicates], thetas[j][report_param], rows, nb_size)
+                for j in range(len(subset))]
+
+    theta = np.array(theta0, np.float64).reshape(chains, D)[subset].copy()
+    n = len(subset)
+    logpost = np.zeros(n)
+    out = np.zeros((iters, n, D))
+    flags = np.zeros((iters, n), bool)
+    try:
+        for j, ll in enumerate(logliks(theta, 0)):
+            logpost[j] = ll if inbox(theta[j]) else -math.inf
+        out[0] = theta
+        flags[0] = True
+        for it in range(1, iters):
+            props = theta.copy()
+            for j, c in enumerate(subset):
+                for d in range(D):
+                    v = _draw(key, STREAM_PROPOSE, c, it, d)
+                    z = math.sqrt(-2.0 * math.log(u01d(v[0], v[1]))) * math.cos(6.283185307179586 * u01d(v[2], v[3]))
+                    props[j, d] = theta[j][d] + steps[it][d] * z
+            lls = logliks(props, it)
+            for j, c in enumerate(subset):
+                lp = lls[j] if inbox(props[j]) else -math.inf
+                v = _draw(key, STREAM_ACCEPT, c, it)
+                acc = lp > -math.inf and math.log(u01d(v[0], v[1])) < lp - logpost[j]
+                if acc:
+                    theta[j] = props[j]
+                    logpost[j] = lp
+                out[it, j] = theta[j]
+                flags[it, j] = acc
+    finally:
+        pool.shutdown()
     return out, flags, logpost

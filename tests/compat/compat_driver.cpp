@@ -158,7 +158,9 @@ int main(int argc, char** argv)
     const uint32_t nInit = (uint32_t)r.nInitialInf, mInit = (uint32_t)r.mInitialInf;
 
     FILE* out = std::fopen(argv[8], "wb");
-    if (!out) return 1;
+    const std::string census_path = std::string(argv[8]) + ".census";
+    FILE* cout_ = std::fopen(census_path.c_str(), "wb");
+    if (!out || !cout_) return 1;
     for (uint32_t run = 0; run < runs; ++run) {
         simulation(nAge, nExp, nHist, nSt, nPle, nRec, nStr, nSub, mAge, mDead, mExp, mSt, mPle, mStr, mSub, nullptr,
                    nIdx, mIdx, nInfSub, mInfSub, nIncSub, nTr, mTr, aoi, aoic, nCnt, mCnt, nLoc, mLoc, nSize, mSize,
@@ -167,8 +169,15 @@ int main(int argc, char** argv)
         for (auto& v : {host(inc, R * S), host(inf, R * S), host(one, R * S), host(ncount, R), host(mcount, R),
                         host(nCnt, P), host(mCnt, P), host(nSize, P), host(mSize, P), host(spatial, (size_t)R * S * P)})
             std::fwrite(v.data(), 4, v.size(), out);
+        // The final census in the reference's types, field by field.
+        auto put = [&](const auto& v) { std::fwrite(v.data(), sizeof(v[0]), v.size(), cout_); };
+        put(host(nAge, N)), put(host(nExp, N)), put(host(nHist, (size_t)N * S)), put(host(nSt, N));
+        put(host(nPle, N)), put(host(nRec, N)), put(host(nStr, N)), put(host(nSub, N)), put(host(nIdx, N));
+        put(host(mAge, M)), put(host(mDead, M)), put(host(mExp, M)), put(host(mSt, M)), put(host(mPle, M));
+        put(host(mStr, M)), put(host(mSub, M)), put(host(mIdx, M));
     }
     std::fclose(out);
+    std::fclose(cout_);
     arbo_compat_release();
     std::printf("seed %llu\n", (unsigned long long)arbo_compat_seed());
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : 3;

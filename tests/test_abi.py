@@ -36,6 +36,8 @@ def test_library_exports_every_declared_symbol(native):
     ("arbo_arch_param", _native.ArchParamStruct),
     ("arbo_io_param", _native.IOParamStruct),
     ("arbo_csr", _native.CSRStruct),
+    ("arbo_mcmc_config", _native.McmcConfigStruct),
+    ("arbo_census_export", _native.CensusExportStruct),
 ])
 def test_struct_layout_matches_header(cname, pystruct):
     assert [f for f, _ in pystruct._fields_] == struct_fields(cname)
