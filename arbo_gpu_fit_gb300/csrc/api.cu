@@ -140,6 +140,9 @@ struct arbo_sim {
     // handle's device (null when the handle exceeds its size or the lookup failed).
     unsigned long long* noalloc = nullptr;
     int noalloc_err = 0;  // cudaError_t of a failed set-up
+    // Fingerprints of the read-only death-age tables (CDF and inverse bucket table), human and
+    // mosquito: handles of one batch with equal tables share one copy in its descriptors.
+    uint64_t tab_h = 0, tab_m = 0;
 };
 
 extern "C" {
@@ -309,6 +312,20 @@ static const char* param_error(const arbo_sim_param& p, uint32_t N, uint32_t M)
         return "seasonal and community-size parameters must be finite";
     if (p.nInitialInf > (float)N || p.mInitialInf > (float)M) return "more initial infections than agents";
     return nullptr;
+}
+
+// FNV-1a fingerprint of a table's bytes and length.
+static uint64_t table_fingerprint(const void* a, size_t na, const void* b, size_t nb)
+{
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* c = (const unsigned char*)p;
+        for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+        for (int k = 0; k < 8; ++k) h = (h ^ ((n >> (8 * k)) & 0xFF)) * 1099511628211ull;
+    };
+    mix(a, na);
+    mix(b, nb);
+    return h;
 }
 
 int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const arbo_io_param* io, const arbo_csr* csr,
@@ -487,6 +504,8 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     UP(d.tcomm, tcomm.data(), (size_t)d.tiles * 4);
     UP(d.csr_loc, csr->loc, (P + 1) * 4);
     if (csr->nnz) UP(d.csr_to, csr->to, (size_t)csr->nnz * 4);
+    s->tab_h = table_fingerprint(cdfh.data(), cdfh.size() * 4, minvh.data(), minvh.size() * 4);
+    s->tab_m = table_fingerprint(cdfm.data(), cdfm.size() * 4, minv.data(), minv.size() * 4);
     UP(d.cdfh, cdfh.data(), cdfh.size() * 4);
     UP(d.cdfm, cdfm.data(), cdfm.size() * 4);
     UP(d.minv, minv.data(), minv.size() * 4);
@@ -1262,6 +1281,7 @@ struct arbo_batch {
     void* flush = nullptr;
     size_t flush_bytes = 0;
     std::vector<uint64_t> versions;  // instance versions the uploaded descriptors reflect
+    std::vector<uint32_t> tab_owner_h, tab_owner_m;  // instance whose tables each instance reads
 };
 
 namespace {
@@ -1279,6 +1299,39 @@ void batch_drop_graphs(arbo_batch* b)
     if (b->gmulti) cudaGraphExecDestroy(b->gmulti);
     if (b->gone) cudaGraphExecDestroy(b->gone);
     b->gmulti = b->gone = nullptr;
+}
+
+// Instances with equal death-age tables (equal life-expectancy parameters and run lengths, as
+// the handles of one MCMC fit) read the tables of the first such instance: one copy stays in the
+// caches instead of one per instance (each rebirth reads a few entries of them).
+void batch_share_tables(arbo_batch* b)
+{
+    const size_t n = b->sims.size();
+    b->tab_owner_h.assign(n, 0);
+    b->tab_owner_m.assign(n, 0);
+    for (size_t i = 0; i < n; ++i) {
+        const arbo_sim* s = b->sims[i];
+        b->tab_owner_h[i] = b->tab_owner_m[i] = (uint32_t)i;
+        for (size_t j = 0; j < i; ++j) {
+            const arbo_sim* o = b->sims[j];
+            if (o->device != s->device) continue;
+            if (b->tab_owner_h[i] == i && o->tab_h == s->tab_h && o->d.ah == s->d.ah) b->tab_owner_h[i] = (uint32_t)j;
+            if (b->tab_owner_m[i] == i && o->tab_m == s->tab_m && o->d.am == s->d.am) b->tab_owner_m[i] = (uint32_t)j;
+        }
+    }
+}
+
+// Descriptor of instance i as the batched kernels read it.
+Dev batch_desc(const arbo_batch* b, size_t i)
+{
+    Dev d = b->sims[i]->d;
+    const Dev& h = b->sims[b->tab_owner_h[i]]->d;
+    const Dev& m = b->sims[b->tab_owner_m[i]]->d;
+    d.cdfh = h.cdfh;
+    d.minvh = h.minvh;
+    d.cdfm = m.cdfm;
+    d.minv = m.minv;
+    return d;
 }
 
 // Block counts of every instance for the launch shapes of `a`; descriptors and tables uploaded.
@@ -1318,8 +1371,9 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     if (!b->mem) CUDA_TRY(cudaMalloc(&b->mem, devb + tab));
     std::vector<Dev> devs(n);
     b->versions.resize(n);
+    batch_share_tables(b);
     for (uint32_t i = 0; i < n; ++i) {
-        devs[i] = b->sims[i]->d;
+        devs[i] = batch_desc(b, i);
         b->versions[i] = b->sims[i]->version;
     }
     std::vector<uint32_t> t;
@@ -1365,7 +1419,8 @@ int batch_refresh(arbo_batch* b)
 {
     for (size_t i = 0; i < b->sims.size(); ++i) {
         if (b->versions[i] == b->sims[i]->version) continue;
-        CUDA_TRY(cudaMemcpy((Dev*)b->mem + i, &b->sims[i]->d, sizeof(Dev), cudaMemcpyHostToDevice));
+        const Dev d = batch_desc(b, i);
+        CUDA_TRY(cudaMemcpy((Dev*)b->mem + i, &d, sizeof(Dev), cudaMemcpyHostToDevice));
         b->versions[i] = b->sims[i]->version;
     }
     return ARBO_OK;

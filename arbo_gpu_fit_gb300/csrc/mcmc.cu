@@ -424,4 +424,24 @@ int arbo_mcmc_chain(arbo_mcmc* h, uint32_t iters, double* out, uint8_t* flags)
     return ARBO_OK;
 }
 
+int arbo_mcmc_restore(arbo_mcmc* h, const double* theta, const double* logpost, const uint32_t* accepted,
+                      const uint32_t* passed, const double* chain, const uint8_t* flags, uint32_t iters, void* stream)
+{
+    if (!h || !theta || !logpost || iters > h->m.iters || (iters && !chain))
+        return mfail(ARBO_ERR_INVALID, "arbo_mcmc_restore: bad arguments");
+    MCUDA(cudaSetDevice(h->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t C = h->m.C, n = C * h->m.D * 8;
+    MCUDA(cudaMemcpyAsync(h->m.theta, theta, n, cudaMemcpyHostToDevice, st));
+    MCUDA(cudaMemcpyAsync(h->m.prop, theta, n, cudaMemcpyHostToDevice, st));
+    MCUDA(cudaMemcpyAsync(h->m.logpost, logpost, C * 8, cudaMemcpyHostToDevice, st));
+    if (accepted) MCUDA(cudaMemcpyAsync(h->m.accepted, accepted, C * 4, cudaMemcpyHostToDevice, st));
+    if (passed) MCUDA(cudaMemcpyAsync(h->m.passed, passed, C * 4, cudaMemcpyHostToDevice, st));
+    if (iters) {
+        MCUDA(cudaMemcpyAsync(h->m.chain, chain, (size_t)iters * n, cudaMemcpyHostToDevice, st));
+        if (flags) MCUDA(cudaMemcpyAsync(h->m.flag, flags, (size_t)iters * C, cudaMemcpyHostToDevice, st));
+    }
+    return cudaStreamSynchronize(st) == cudaSuccess ? ARBO_OK : mfail(ARBO_ERR_CUDA, "sync");
+}
+
 }  // extern "C"

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes
 import time
+from dataclasses import dataclass, field
 from ctypes import POINTER, byref, c_uint32, c_void_p
 from typing import Callable, List, Optional
 
@@ -185,6 +186,20 @@ class MCMC:
         check(self._lib.arbo_mcmc_chain(self._h, int(iters), _dp(out), fl.ctypes.data_as(POINTER(ctypes.c_uint8))))
         return out, fl.astype(bool)
 
+    def restore(self, ck: "Checkpoint") -> None:
+        """Puts back the chains' state of a checkpoint (arbo_mcmc_restore) and its step sizes."""
+        th = np.ascontiguousarray(ck.theta, np.float64)
+        lp = np.ascontiguousarray(ck.logpost, np.float64)
+        acc = np.ascontiguousarray(ck.accepted, np.uint32)
+        pas = np.ascontiguousarray(ck.passed, np.uint32)
+        n = min(int(ck.chain.shape[0]), self.max_iters)
+        ch = np.ascontiguousarray(ck.chain[:n], np.float64)
+        fl = np.ascontiguousarray(ck.flags[:n], np.uint8)
+        check(self._lib.arbo_mcmc_restore(self._h, _dp(th), _dp(lp), acc.ctypes.data_as(POINTER(c_uint32)),
+                                          pas.ctypes.data_as(POINTER(c_uint32)), _dp(ch),
+                                          fl.ctypes.data_as(POINTER(ctypes.c_uint8)), n, None))
+        self.set_step(ck.step)
+
     # -- helpers shared by the drivers ----------------------------------------------------
     def make_sims(self, n: int) -> List[Simulation]:
         w = self.workload
@@ -234,6 +249,14 @@ class StepAdapter:
             self.steps[it + 1] = m.step_sd.copy()
         self.last = acc
 
+    def state(self) -> dict:
+        return {"last": self.last, "history": list(self.history), "steps": {k: v.tolist() for k, v in self.steps.items()}}
+
+    def load(self, st: dict) -> None:
+        self.last = st.get("last")
+        self.history = [tuple(h) for h in st.get("history", [])]
+        self.steps = {int(k): np.asarray(v, np.float64) for k, v in st.get("steps", {}).items()}
+
     def schedule(self, step0: np.ndarray, iters: int) -> np.ndarray:
         """Standard deviations used by the proposal of every iteration, [iters, D]."""
         out = np.zeros((iters, len(step0)))
@@ -242,6 +265,67 @@ class StepAdapter:
             cur = self.steps.get(it, cur)
             out[it] = cur
         return out
+
+
+@dataclass
+class Checkpoint:
+    """The state of every chain after iteration `it`: enough for a new MCMC handle to continue the
+    chains exactly (arbo_mcmc_restore), together with the recorded chain so far and the burn-in
+    adaptation."""
+    it: int
+    theta: np.ndarray
+    logpost: np.ndarray
+    accepted: np.ndarray
+    passed: np.ndarray
+    step: np.ndarray
+    chain: np.ndarray
+    flags: np.ndarray
+    adapt: dict = field(default_factory=dict)
+
+
+def take_checkpoint(m: "MCMC", it: int, adapt: Optional["StepAdapter"] = None) -> Checkpoint:
+    st = m.state()
+    chain, flags = m.chain(min(it + 1, m.max_iters))
+    return Checkpoint(int(it), st["theta"], st["logpost"], st["accepted"], st["passed"], m.step_sd.copy(), chain,
+                      flags, adapt.state() if adapt else {})
+
+
+def save_checkpoint(path: str, ck: Checkpoint) -> None:
+    """Writes the checkpoint (npz, replaced atomically)."""
+    import json
+    import os
+
+    tmp = path + ".tmp.npz"
+    np.savez_compressed(tmp, it=ck.it, theta=ck.theta, logpost=ck.logpost, accepted=ck.accepted, passed=ck.passed,
+                        step=ck.step, chain=ck.chain, flags=ck.flags, adapt=json.dumps(ck.adapt))
+    os.replace(tmp, path)
+
+
+def load_checkpoint(path: str) -> Checkpoint:
+    import json
+
+    z = np.load(path)
+    return Checkpoint(int(z["it"]), z["theta"], z["logpost"], z["accepted"], z["passed"], z["step"], z["chain"],
+                      z["flags"], json.loads(str(z["adapt"])))
+
+
+class Checkpointer:
+    """on_iter callback of the drivers that writes a checkpoint every `every` iterations."""
+
+    def __init__(self, m: "MCMC", path: str, every: int, adapt: Optional["StepAdapter"] = None):
+        self.m, self.path, self.every, self.adapt = m, path, max(1, int(every)), adapt
+
+    def __call__(self, it: int) -> None:
+        if it > 0 and it % self.every == 0:
+            save_checkpoint(self.path, take_checkpoint(self.m, it, self.adapt))
+
+
+def _resume(m: "MCMC", resume: Checkpoint, adapt: Optional["StepAdapter"]) -> int:
+    """Restores a checkpoint into m (and the adapter); returns the first iteration to run."""
+    m.restore(resume)
+    if adapt is not None:
+        adapt.load(resume.adapt)
+    return resume.it + 1
 
 
 def _simulate_alone(sim: Simulation):
@@ -269,16 +353,22 @@ def start(m: MCMC, theta0: np.ndarray, sims: List[Simulation], batch: Optional[B
 
 
 def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
-              on_iter: Optional[Callable] = None, adapt: Optional[StepAdapter] = None) -> dict:
+              on_iter: Optional[Callable] = None, adapt: Optional[StepAdapter] = None,
+              resume: Optional[Checkpoint] = None) -> dict:
     """One proposal at a time: for every chain in turn, its proposal is simulated by the same
-    handle(s) (replicates of one handle each) and accepted or rejected."""
+    handle(s) (replicates of one handle each) and accepted or rejected. With `resume`, the chains
+    continue from a checkpoint instead of starting at theta0."""
     sims = sims if sims is not None else m.make_sims(m.R)
     t0 = time.perf_counter()
-    start(m, theta0, sims)
-    if on_iter:
-        on_iter(0)
+    if resume is None:
+        start(m, theta0, sims)
+        it0 = 1
+        if on_iter:
+            on_iter(0)
+    else:
+        it0 = _resume(m, resume, adapt)
     sim_s = 0.0
-    for it in range(1, iters):
+    for it in range(it0, iters):
         prop = m.propose(it)
         for c in range(m.C):
             t1 = time.perf_counter()
@@ -292,23 +382,28 @@ def run_plain(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simul
             adapt(m, it)
         if on_iter:
             on_iter(it)
-    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * iters}
+    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * (iters - it0 + 1)}
 
 
 def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Simulation]] = None,
                 batch: Optional[Batch] = None, on_iter: Optional[Callable] = None,
-                adapt: Optional[StepAdapter] = None) -> dict:
+                adapt: Optional[StepAdapter] = None, resume: Optional[Checkpoint] = None) -> dict:
     """All chains together: the proposals of the C chains (times replicates) are simulated by one
-    batch, then the likelihoods and the acceptance steps of all chains run as one kernel each."""
+    batch, then the likelihoods and the acceptance steps of all chains run as one kernel each.
+    With `resume`, the chains continue from a checkpoint."""
     sims = sims if sims is not None else m.make_sims(m.C * m.R)
     own = batch is None
     batch = batch if batch is not None else chain_batch(sims)
     t0 = time.perf_counter()
-    start(m, theta0, sims, batch)
-    if on_iter:
-        on_iter(0)
+    if resume is None:
+        start(m, theta0, sims, batch)
+        it0 = 1
+        if on_iter:
+            on_iter(0)
+    else:
+        it0 = _resume(m, resume, adapt)
     sim_s = 0.0
-    for it in range(1, iters):
+    for it in range(it0, iters):
         prop = m.propose(it)
         for c in range(m.C):
             for r in range(m.R):
@@ -325,12 +420,12 @@ def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Sim
             on_iter(it)
     if own:
         batch.close()
-    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * iters}
+    return {"wall_s": time.perf_counter() - t0, "sim_s": sim_s, "simulations": m.C * m.R * (iters - it0 + 1)}
 
 
 def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np.ndarray], np.ndarray],
                 sims: Optional[List[Simulation]] = None, on_iter: Optional[Callable] = None,
-                adapt: Optional[StepAdapter] = None) -> dict:
+                adapt: Optional[StepAdapter] = None, resume: Optional[Checkpoint] = None) -> dict:
     """Delayed-acceptance Metropolis-Hastings (Christen & Fox 2005). ``surrogate(theta[C, D])``
     returns an approximate log-likelihood per chain. Stage 1 screens every proposal with it (GPU,
     FP64); only the proposals that pass are simulated, together in one batch of as many handles as
@@ -339,16 +434,22 @@ def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np
     only on its simulated likelihood."""
     sims = sims if sims is not None else m.make_sims(m.C * m.R)
     t0 = time.perf_counter()
-    theta0 = np.asarray(theta0, np.float64).reshape(m.C, m.D)
-    with chain_batch(sims) as b0:
-        start(m, theta0, sims, b0)
-    m.set_screen(surrogate(theta0), surrogate(theta0))
-    if on_iter:
-        on_iter(0)
-    sim_s, simulated = 0.0, m.C * m.R
+    if resume is None:
+        theta0 = np.asarray(theta0, np.float64).reshape(m.C, m.D)
+        with chain_batch(sims) as b0:
+            start(m, theta0, sims, b0)
+        m.set_screen(surrogate(theta0), surrogate(theta0))
+        it0, simulated = 1, m.C * m.R
+        if on_iter:
+            on_iter(0)
+    else:
+        it0, simulated = _resume(m, resume, adapt), 0
+        cur = np.asarray(resume.theta, np.float64).reshape(m.C, m.D)
+        m.set_screen(surrogate(cur), surrogate(cur))  # the surrogate is deterministic
+    sim_s = 0.0
     batches = {}
     try:
-        for it in range(1, iters):
+        for it in range(it0, iters):
             prop = m.propose(it)
             m.set_screen(surrogate(prop))
             passed = np.flatnonzero(m.screen(it))

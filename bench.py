@@ -178,13 +178,22 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def ref_workload(small, seed, max_time=3650):
+    """The workload of the CPU legs, built without loading the library they are compared with
+    (oracle/workloads.py; the profiling-sized case comes from the package's configs)."""
+    if small:
+        from arbo_gpu_fit_gb300 import configs
+        return configs.scaled(125_000, 750_000, 18, max_time, seed=seed)
+    from oracle import workloads
+    return workloads.plain_large(seed=seed, max_time=max_time)
+
+
 def run_oracle_sample(args_tuple):
     """One CPU replica: init (untimed) + `steps` oracle steps (timed). Runs in a spawned process."""
     steps, seed, small = args_tuple
     sys.path.insert(0, str(ROOT))
-    from arbo_gpu_fit_gb300 import configs
     from oracle.binding import OracleSim
-    w = configs.scaled(125_000, 750_000, 18, 3650, seed=seed) if small else configs.plain_large(seed=seed)
+    w = ref_workload(small, seed)
     o = OracleSim(w.parameter.simulation, w.network, w.n_sizes, w.m_sizes, w.max_time, w.seed)
     o.init()
     t0 = time.perf_counter()
@@ -209,7 +218,7 @@ def reference_arm(args, world, rank):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    w = workload(args, 20261203)
+    w = ref_workload(args.small, 20261203, max(3650, args.warmup + args.steps))
     rate, per_step_ms, agents = cpu_baseline(args, cores)
     sample = (f"{cores} independent replicas of the workload, each: init (untimed) + {args.cpu_steps} "
               f"serial steps (timed), oracle/ restatement of the reference's per-step logic")

@@ -531,6 +531,15 @@ int arbo_mcmc_state(arbo_mcmc* m, double* theta, double* logpost, double* loglik
                     uint32_t* passed);
 /* Recorded states of the first iters iterations ([iter][chain][param]) and accept flags. */
 int arbo_mcmc_chain(arbo_mcmc* m, uint32_t iters, double* out, uint8_t* flags);
+/* Checkpoint / resume: puts back the state a checkpoint took with arbo_mcmc_state and
+ * arbo_mcmc_chain, so that a new handle continues a chain exactly (every random number is keyed by
+ * chain and iteration): current states and log posteriors (chains x params, chains), accepted and
+ * first-stage-passed counts (optional), and the first `iters` recorded iterations with their flags
+ * (optional; iters <= max_iters). The log posteriors are restored, not re-estimated: a
+ * pseudo-marginal chain keeps the estimate it accepted. No reference counterpart: the reference
+ * appends its chain files every step (cpp/MCMC.cpp:400-484) but cannot restart from them. */
+int arbo_mcmc_restore(arbo_mcmc* m, const double* theta, const double* logpost, const uint32_t* accepted,
+                      const uint32_t* passed, const double* chain, const uint8_t* flags, uint32_t iters, void* stream);
 
 /* ------------------------------------------------------------------ surrogate */
 
