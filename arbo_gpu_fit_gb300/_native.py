@@ -143,6 +143,7 @@ SIGNATURES = {
     "arbo_mcmc_screen": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_uint8), c_void_p]),
     "arbo_mcmc_state": (c_int, [c_void_p, POINTER(ctypes.c_double), POINTER(ctypes.c_double), POINTER(ctypes.c_double), POINTER(c_uint32), POINTER(c_uint32)]),
     "arbo_mcmc_chain": (c_int, [c_void_p, c_uint32, POINTER(ctypes.c_double), POINTER(ctypes.c_uint8)]),
+    "arbo_mcmc_set_proposal": (c_int, [c_void_p, POINTER(ctypes.c_double), ctypes.c_double]),
     "arbo_mcmc_restore": (c_int, [c_void_p, POINTER(ctypes.c_double), POINTER(ctypes.c_double), POINTER(c_uint32),
                                   POINTER(c_uint32), POINTER(ctypes.c_double), POINTER(ctypes.c_uint8), c_uint32,
                                   c_void_p]),

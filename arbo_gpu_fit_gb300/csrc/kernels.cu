@@ -73,64 +73,9 @@ __device__ __forceinline__ Key load_key(const Ctrl* c)
     return k;
 }
 
-// Counter deltas of the rare per-agent paths (transitions, deaths of infected agents), queued per
-// warp in shared memory and applied at the warp's next convergence point with one atomic per
-// distinct counter (a warp's agents lie in one or two communities, so their deltas share
-// counters). Key: counter array in the top two bits, index below.
-constexpr uint32_t kCounterQueue = 64;
-enum : uint32_t { kCtrInfh = 0, kCtrInc = 1, kCtrInfm = 2 };
-
-struct CounterQueue {
-    uint32_t n;
-    uint32_t key[kCounterQueue];
-    int32_t delta[kCounterQueue];
-};
-
-// Applies delta to counter (arr, idx); a decrement that would take it below zero records
-// ARBO_DEVERR_COUNTER.
-__device__ __forceinline__ void counter_apply(const Dev& d, uint32_t arr, uint32_t idx, int delta)
+__device__ __forceinline__ void counter_dec(uint32_t* p, Ctrl* ctrl)
 {
-    uint32_t* p = (arr == kCtrInfh ? d.infh : arr == kCtrInc ? d.inc : d.infm) + idx;
-    if (delta > 0) {
-        atomicAdd(p, (uint32_t)delta);
-    } else if (delta < 0) {
-        const uint32_t m = (uint32_t)(-delta);
-        if (atomicSub(p, m) < m) atomicOr(&d.ctrl->err, ARBO_DEVERR_COUNTER);
-    }
-}
-
-// Any lane, converged or not: queues a delta (applied at once when the queue is full).
-__device__ __forceinline__ void counter_push(CounterQueue& q, const Dev& d, uint32_t arr, uint32_t idx, int delta)
-{
-    const uint32_t k = atomicAdd(&q.n, 1u);
-    if (k < kCounterQueue) {
-        q.key[k] = (arr << 30) | idx;
-        q.delta[k] = delta;
-    } else {
-        counter_apply(d, arr, idx, delta);
-    }
-}
-
-// The whole warp, converged: sums the queued deltas per counter (warp match and reduction) and
-// applies each sum with one atomic; empties the queue.
-__device__ __forceinline__ void counter_flush(CounterQueue& q, const Dev& d, uint32_t lane)
-{
-    __syncwarp();
-    const uint32_t n = min(q.n, kCounterQueue);
-    for (uint32_t b = 0; b < n; b += 32) {
-        const bool has = b + lane < n;
-        const uint32_t key = has ? q.key[b + lane] : 0u;
-        const int dv = has ? q.delta[b + lane] : 0;
-        const unsigned act = __ballot_sync(0xFFFFFFFFu, has);
-        if (has) {
-            const unsigned grp = __match_any_sync(act, key);
-            const int sum = __reduce_add_sync(grp, dv);
-            if (lane == (uint32_t)(__ffs(grp) - 1) && sum != 0) counter_apply(d, key >> 30, key & 0x3FFFFFFFu, sum);
-        }
-    }
-    __syncwarp();
-    if (lane == 0) q.n = 0;
-    __syncwarp();
+    if (atomicSub(p, 1u) == 0u) atomicOr(&ctrl->err, ARBO_DEVERR_COUNTER);
 }
 
 __device__ __forceinline__ unsigned long long order_key(uint32_t hiword, uint32_t j, uint32_t intro, uint32_t e)
@@ -171,11 +116,16 @@ __device__ __forceinline__ uint32_t human_comm(const uint32_t* __restrict__ nloc
 // a transition of an exposed or infectious human or a death with rebirth. `ex` / `rec` are its
 // exposed and recovery ages and `born` its birth time (its age is tn - born). Returns the new
 // status byte in the low word and the human's new next event time in the high word.
-__device__ __noinline__ unsigned long long human_slow(const Dev& d, CounterQueue& q, uint32_t i, uint32_t st, int32_t tn,
-                                                      int32_t dtime, int32_t born, int32_t ex, int32_t rec, uint32_t t,
-                                                      Key key)
+__device__ __noinline__ unsigned long long human_slow(uint32_t i, uint32_t st, int32_t tn, int32_t dtime, int32_t born,
+                                                      int32_t ex, int32_t rec, uint32_t t,
+                                                      const uint32_t* __restrict__ nloc,
+                                                      const uint32_t* __restrict__ hcomm, uint32_t P,
+                                                      const uint8_t* n_strain, float* n_ple, int32_t* n_born,
+                                                      int32_t* n_dtime, uint8_t* n_imm, uint32_t* infh, uint32_t* inc,
+                                                      const float* __restrict__ cdfh,
+                                                      const uint32_t* __restrict__ minvh, uint32_t ah, Key key,
+                                                      Ctrl* ctrl)
 {
-    const uint32_t P = d.P;
     auto pack = [](uint32_t status, int32_t next) {
         return ((unsigned long long)(uint32_t)next << 32) | status;
     };
@@ -183,32 +133,32 @@ __device__ __noinline__ unsigned long long human_slow(const Dev& d, CounterQueue
         const int32_t a = tn - born;
         if (st == 2) {
             if (rec < a) {
-                const uint32_t c = human_comm(d.nloc, d.hcomm, P, i);
-                counter_push(q, d, kCtrInfh, d.n_strain[i] * P + c, -1);
+                const uint32_t c = human_comm(nloc, hcomm, P, i);
+                counter_dec(&infh[n_strain[i] * P + c], ctrl);
                 return pack(0, dtime);
             }
         } else if (st == 1) {
             if (ex < a) {
-                const uint32_t c = human_comm(d.nloc, d.hcomm, P, i);
-                const uint32_t s = d.n_strain[i];
-                counter_push(q, d, kCtrInc, s * P + c, 1);
-                counter_push(q, d, kCtrInfh, s * P + c, 1);
+                const uint32_t c = human_comm(nloc, hcomm, P, i);
+                const uint32_t s = n_strain[i];
+                atomicAdd(&inc[s * P + c], 1u);
+                atomicAdd(&infh[s * P + c], 1u);
                 return pack(2, human_next(2, dtime, born, rec));
             }
         }
         return pack(st, human_next(st, dtime, born, st == 1 ? ex : rec));
     }
     if (st == 2) {
-        const uint32_t c = human_comm(d.nloc, d.hcomm, P, i);
-        counter_push(q, d, kCtrInfh, d.n_strain[i] * P + c, -1);
+        const uint32_t c = human_comm(nloc, hcomm, P, i);
+        counter_dec(&infh[n_strain[i] * P + c], ctrl);
     }
     const U4 r = draw4(key, kHumanRebirth, i >> 2, t);
     const float ple = u01(r.v[i & 3]);
-    const int32_t dt = death_time(tn, death_age_inv(d.cdfh, d.minvh, d.ah, ple, 65536.0f));
-    d.n_ple[i] = ple;
-    d.n_born[i] = tn;
-    d.n_dtime[i] = dt;
-    d.n_imm[i] = 0;
+    const int32_t dt = death_time(tn, death_age_inv(cdfh, minvh, ah, ple, 65536.0f));
+    n_ple[i] = ple;
+    n_born[i] = tn;
+    n_dtime[i] = dt;
+    n_imm[i] = 0;
     return pack(0, dt);
 }
 
@@ -218,8 +168,7 @@ __device__ __noinline__ unsigned long long human_slow(const Dev& d, CounterQueue
 // streams only that time. A group with an event due loads its status, times and ages in one round
 // trip and takes the slow path for the humans whose event is due.
 template <int U>
-__device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32_t g0, uint32_t stride, uint32_t t,
-                                             CounterQueue& q)
+__device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32_t g0, uint32_t stride, uint32_t t)
 {
     int4 X[U];
     bool ok[U];
@@ -246,14 +195,15 @@ __device__ __forceinline__ void demog_humans(const Dev& d, const Key key, uint32
         for (int k = 0; k < 4; ++k) {
             if (tn < xv[k]) continue;
             const uint32_t st = (sw >> (8 * k)) & 0xFFu;
-            const unsigned long long res = human_slow(d, q, 4 * g + k, st, tn, dd[k], bv[k], ev[k], rv[k], t, key);
+            const unsigned long long res =
+                human_slow(4 * g + k, st, tn, dd[k], bv[k], ev[k], rv[k], t, d.nloc, d.hcomm, d.P, d.n_strain, d.n_ple,
+                           d.n_born, d.n_dtime, d.n_imm, d.infh, d.inc, d.cdfh, d.minvh, d.ah, key, d.ctrl);
             nsw = (nsw & ~(0xFFu << (8 * k))) | (((uint32_t)res & 0xFFu) << (8 * k));
             nx[k] = (int32_t)(uint32_t)(res >> 32);
         }
         if (nsw != sw) reinterpret_cast<unsigned int*>(d.n_status)[g] = nsw;
         reinterpret_cast<int4*>(d.n_next)[g] = make_int4(nx[0], nx[1], nx[2], nx[3]);
     }
-    counter_flush(q, d, threadIdx.x & 31u);  // the group's transitions and deaths of infected humans
 }
 
 __device__ __forceinline__ uint32_t slot_comm(const Dev& d, uint32_t c0, uint32_t i)
@@ -263,12 +213,14 @@ __device__ __forceinline__ uint32_t slot_comm(const Dev& d, uint32_t c0, uint32_
     return c;
 }
 
-// Rare per-mosquito counter change (death of an infectious mosquito, or E->I), queued.
-__device__ __noinline__ void mosq_counter(const Dev& d, CounterQueue& q, uint32_t i, int add)
+// Rare per-mosquito counter change (death of an infectious mosquito, or E->I).
+__device__ __noinline__ void mosq_counter(uint32_t* infm, const uint8_t* m_strain, const uint32_t* __restrict__ mloc,
+                                          const uint32_t* __restrict__ tcomm, uint32_t P, uint32_t i, int add, Ctrl* ctrl)
 {
-    uint32_t c = __ldg(&d.tcomm[i / kTile]);
-    while (c + 1 < d.P && __ldg(&d.mloc[c + 1]) <= i) ++c;
-    counter_push(q, d, kCtrInfm, d.m_strain[i] * d.P + c, add);
+    uint32_t c = __ldg(&tcomm[i / kTile]);
+    while (c + 1 < P && __ldg(&mloc[c + 1]) <= i) ++c;
+    uint32_t* p = &infm[m_strain[i] * P + c];
+    if (add > 0) atomicAdd(p, 1u); else counter_dec(p, ctrl);
 }
 
 
@@ -288,7 +240,6 @@ __device__ __forceinline__ uint32_t pick4(const U4& v, uint32_t i)
 struct QuadSmem {
     uint4 draw[kQuad][32];
     uint8_t slot[kQuad][kTile];
-    CounterQueue cq;  // counter deltas of the warp (human groups or mosquito quads)
 };
 
 // The m lowest set bits of a 4-bit mask, from 64-bit tables of sixteen 4-bit entries.
@@ -365,11 +316,11 @@ __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, 
             const uint32_t i = 4 * g + k;
             const uint32_t st = (ns >> (8 * k)) & 0xFFu;
             if (st & kDead) {
-                if ((st & 3u) == 2u) mosq_counter(d, sm.cq, i, -1);
+                if ((st & 3u) == 2u) mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, -1, d.ctrl);
             } else if ((st & 3u) == 1u) {
                 if (d.m_exposed[i] < tn - d.m_born[i]) {
                     ns = (ns & ~(0x3u << (8 * k))) | (2u << (8 * k));
-                    mosq_counter(d, sm.cq, i, +1);
+                    mosq_counter(d.infm, d.m_strain, d.mloc, d.tcomm, d.P, i, +1, d.ctrl);
                 }
             }
         }
@@ -482,7 +433,7 @@ __device__ __forceinline__ void mosquito_quad_core(const Dev& d, const Key key, 
         d.m_born[i] = tn;
         d.m_dtime[i] = death_time(tn, death_age_inv(d.cdfm, d.minv, d.am, ple, 4096.0f));
     }
-    counter_flush(sm.cq, d, lane);  // the quad's infectious deaths and transitions
+    __syncwarp();
 }
 
 // Quad with its census words loaded straight from global memory.
@@ -597,10 +548,8 @@ __global__ void __launch_bounds__(128, 4) k_demog_tma(Dev d, uint32_t koff)
         if (gw < quads) issue_quad(d, gw, ws.stage[0], &ws.mbar[0]);
     }
     __syncwarp();
-    if (lane == 0) ws.qs.cq.n = 0;
-    __syncwarp();
     const uint32_t hchunks = (d.nvec + 32 * U - 1) / (32 * U);
-    for (uint32_t ch = gw; ch < hchunks; ch += nw) demog_humans<U>(d, key, ch * 32 * U + lane, 32, t, ws.qs.cq);
+    for (uint32_t ch = gw; ch < hchunks; ch += nw) demog_humans<U>(d, key, ch * 32 * U + lane, 32, t);
     uint32_t phase = 0;  // bit s: parity to wait for on stage s
     uint32_t i = 0;
     for (uint32_t q = gw; q < quads; q += nw, ++i) {
@@ -643,10 +592,8 @@ __device__ __forceinline__ void demog_block(const Dev& d, uint32_t b, uint32_t h
 {
     const uint32_t t = d.ctrl->t + koff;
     const Key key = load_key(d.ctrl);
-    if ((threadIdx.x & 31u) == 0) wsm[threadIdx.x >> 5].cq.n = 0;
-    __syncwarp();
     if (b < hblocks) {
-        demog_humans<U>(d, key, b * blockDim.x * U + threadIdx.x, blockDim.x, t, wsm[threadIdx.x >> 5].cq);
+        demog_humans<U>(d, key, b * blockDim.x * U + threadIdx.x, blockDim.x, t);
     } else {
         const uint32_t wpb = blockDim.x >> 5;
         const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -738,7 +685,7 @@ __device__ __forceinline__ void foi_warp(const Dev& d, uint32_t p0, int collect_
         uint32_t ih = d.infh[p], im = d.infm[p], ic = d.inc[p];
         uint32_t mcc = d.mcnt[c];
         if (ic) d.inc[p] = 0u;
-        // A count at or above 2^31 is a counter that went below zero (counter_apply records
+        // A count at or above 2^31 is a counter that went below zero (counter_dec records
         // ARBO_DEVERR_COUNTER when that happens): it is read as 0, so that an inconsistent state
         // cannot turn into an unbounded number of events.
         if ((ih | im | ic | mcc) & 0x80000000u) {
@@ -805,42 +752,28 @@ __device__ __forceinline__ void foi_warp(const Dev& d, uint32_t p0, int collect_
     sh.base[lane] = v - own;
     if (lane == 31) sh.base[32] = v;
     __syncwarp();
-    // Every lane runs the same number of passes (the warp stays converged), so the events of a pass
-    // that share a destination (a source's few CSR neighbours, its own community) are counted by
-    // a warp match and added with one atomic per destination.
     const uint32_t G = sh.base[32];
-    for (uint32_t g0 = 0; g0 < G; g0 += 32) {
-        const uint32_t gi = g0 + lane;
-        uint32_t dkey[4] = {UINT_MAX, UINT_MAX, UINT_MAX, UINT_MAX};  // bit 31: events on humans
-        if (gi < G) {
-            uint32_t lo = 0, hi = 31;  // last lane whose first group is <= gi
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (sh.base[mid] <= gi) lo = mid; else hi = mid - 1;
-            }
-            const uint32_t owner = lo, rel = gi - sh.base[owner];
-            const uint32_t kind =
-                rel >= sh.kofs[owner][3] ? 3u : rel >= sh.kofs[owner][2] ? 2u : rel >= sh.kofs[owner][1] ? 1u : 0u;
-            const uint32_t r4 = rel - sh.kofs[owner][kind];
-            const uint32_t po = p0 + owner, so = po / P;
-            const uint32_t n = sh.cnt[owner][kind];
-            const uint32_t stream = kind == 0 ? kFoiHMLocal : kind == 1 ? kFoiHMLong : kind == 2 ? kFoiMHLocal : kFoiMHLong;
-            const U4 r = draw4(key, stream, po, t, r4);
-            const uint32_t lo_ = sh.loc[owner], dg = sh.deg[owner];
-#pragma unroll
-            for (int qq = 0; qq < 4; ++qq) {
-                if (4 * r4 + qq >= n) break;
-                const uint32_t nb = (kind & 1u) ? 0u : bounded(r.v[qq], dg);
-                const uint32_t dest =
-                    (kind & 1u) ? bounded(r.v[qq], P) : (dg <= 8 ? sh.to[owner][nb] : __ldg(&d.csr_to[lo_ + nb]));
-                dkey[qq] = (kind < 2 ? 0u : 0x80000000u) | (so * P + dest);
-            }
+    for (uint32_t gi = lane; gi < G; gi += 32) {
+        uint32_t lo = 0, hi = 31;  // last lane whose first group is <= gi
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (sh.base[mid] <= gi) lo = mid; else hi = mid - 1;
         }
+        const uint32_t owner = lo, rel = gi - sh.base[owner];
+        const uint32_t kind = rel >= sh.kofs[owner][3] ? 3u : rel >= sh.kofs[owner][2] ? 2u : rel >= sh.kofs[owner][1] ? 1u : 0u;
+        const uint32_t r4 = rel - sh.kofs[owner][kind];
+        const uint32_t po = p0 + owner, so = po / P;
+        const uint32_t n = sh.cnt[owner][kind];
+        const uint32_t stream = kind == 0 ? kFoiHMLocal : kind == 1 ? kFoiHMLong : kind == 2 ? kFoiMHLocal : kFoiMHLong;
+        uint32_t* trans = kind < 2 ? d.transm : d.transh;
+        const U4 r = draw4(key, stream, po, t, r4);
+        const uint32_t lo_ = sh.loc[owner], dg = sh.deg[owner];
 #pragma unroll
         for (int qq = 0; qq < 4; ++qq) {
-            const unsigned grp = __match_any_sync(kFull, dkey[qq]);
-            if (dkey[qq] != UINT_MAX && lane == (uint32_t)(__ffs(grp) - 1))
-                atomicAdd(&((dkey[qq] >> 31) ? d.transh : d.transm)[dkey[qq] & 0x7FFFFFFFu], (uint32_t)__popc(grp));
+            if (4 * r4 + qq >= n) break;
+            const uint32_t nb = (kind & 1u) ? 0u : bounded(r.v[qq], dg);
+            const uint32_t dest = (kind & 1u) ? bounded(r.v[qq], P) : (dg <= 8 ? sh.to[owner][nb] : __ldg(&d.csr_to[lo_ + nb]));
+            atomicAdd(&trans[so * P + dest], 1u);
         }
     }
     __syncwarp();  // the tables are reused for the warp's next pairs
@@ -954,35 +887,6 @@ __device__ __forceinline__ void infect_warp(const Dev& d, uint32_t c, uint32_t k
     // One draw per lane in one pass: introduction counts (lanes < S), first serotypes (8, 9).
     const U4 rd = draw4(key, lane < S ? (uint32_t)kIntroCount : lane == 8 ? (uint32_t)kInfMStart : (uint32_t)kInfHStart,
                         lane < S ? pl : c, t);
-    // While the force-of-infection kernel runs: the first target group of every serotype position
-    // (its draws do not depend on the event counts) has its census words fetched into L2, so the
-    // bids and the winners' reads after the wait find them there. Prefetches return nothing, so
-    // what the demographic or force-of-infection kernels still write does not matter here.
-    {
-        const uint32_t h0 = __shfl_sync(kFull, bounded(rd.v[0], S), 9), m0 = __shfl_sync(kFull, bounded(rd.v[0], S), 8);
-        const bool hum = lane < S && ns != 0, mos = lane >= 16 && lane < 16 + S && ms != 0;
-        if (hum || mos) {
-            const uint32_t j = hum ? lane : lane - 16;
-            const uint32_t sp = ((hum ? h0 : m0) + j) % S;
-            const U4 r = draw4(key, hum ? (uint32_t)kInfHTarget : (uint32_t)kInfMTarget, sp * P + c, t, 0);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (hum) {
-                    const uint32_t i = nbase + bounded(r.v[q], ns);
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.n_status + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.n_imm + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.winh + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.n_born + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.n_dtime + i));
-                } else {
-                    const uint32_t i = mbase + bounded(r.v[q], ms);
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.m_state + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.winm + i));
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(d.m_born + i));
-                }
-            }
-        }
-    }
     griddep_wait();
     const uint32_t mc = d.mcnt[c];
     uint32_t kh = lane < S ? d.transh[pl] : 0u;
@@ -1237,8 +1141,6 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
     const Dev& d = *reinterpret_cast<const Dev*>(wdev[warp]);
     const uint32_t total = __ldg(&bd.demog_off[bd.n]);
     uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its item range
-    if (lane == 0) wsm[warp].cq.n = 0;
-    __syncwarp();
     for (;;) {
         uint32_t it0 = 0;
         if (lane == 0) it0 = atomicAdd(bd.work, 2u);
@@ -1259,7 +1161,7 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
             const uint32_t local = it - lo, hw = __ldg(&bd.demog_h[inst]);
             const uint32_t t = d.ctrl->t + koff;
             const Key key = load_key(d.ctrl);
-            if (local < hw) demog_humans<U>(d, key, local * 32 * U + lane, 32, t, wsm[warp].cq);
+            if (local < hw) demog_humans<U>(d, key, local * 32 * U + lane, 32, t);
             else demog_mosquito_quad(d, key, local - hw, lane, t, wsm[warp]);
         }
     }

@@ -30,6 +30,9 @@ struct McmcDev {
     const double* lo;          // [D]
     const double* hi;          // [D]
     const double* step;        // [D] random-walk standard deviations
+    const double* chol;        // [D*D] lower Cholesky factor of the adapted proposal covariance
+    double beta;               // weight of the diagonal part when chol is in use
+    uint32_t use_cov;          // 1: proposals use chol (arbo_mcmc_set_proposal)
     const uint32_t* y;         // [Mo*S] observed cases, month-major
     const uint32_t* mrow;      // [Mo+1] first daily-series row of each month
     double* theta;             // [C*D] current state
@@ -60,17 +63,37 @@ __device__ __forceinline__ bool in_box(const McmcDev& m, const double* th)
     return true;
 }
 
-// Random-walk proposals: theta + step * z, z standard normal by Box-Muller from one Philox call.
+// Standard normal number k of chain c at iteration iter (Box-Muller on one Philox call).
+__device__ __forceinline__ double normal_draw(const McmcDev& m, uint32_t c, uint32_t iter, uint32_t k)
+{
+    const Key key{m.k0, m.k1, 0};
+    const U4 r = draw4(key, kMcmcPropose, c, iter, k);
+    const double u1 = u01d(r.v[0], r.v[1]), u2 = u01d(r.v[2], r.v[3]);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// Proposals, one thread per chain (MCMC::propose, cpp/MCMC.cpp:108-161). Diagonal random walk:
+// theta + step * z0. With an adapted covariance (adaptive Metropolis, Roberts & Rosenthal 2009, as
+// the reference's after 100 * params steps): theta + beta * step * z0 + (1 - beta) * L z1, L the
+// Cholesky factor of 2.38^2 / params times the chains' covariance; z0 and z1 are independent
+// standard normal vectors (draws d and 32 + d of the chain and iteration).
 __global__ void k_propose(McmcDev m, uint32_t iter)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.C * m.D) return;
-    const uint32_t c = i / m.D, d = i - c * m.D;
-    const Key key{m.k0, m.k1, 0};
-    const U4 r = draw4(key, kMcmcPropose, c, iter, d);
-    const double u1 = u01d(r.v[0], r.v[1]), u2 = u01d(r.v[2], r.v[3]);
-    const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
-    m.prop[i] = m.theta[i] + m.step[d] * z;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.C) return;
+    const double* th = m.theta + (size_t)c * m.D;
+    double* pr = m.prop + (size_t)c * m.D;
+    if (!m.use_cov) {
+        for (uint32_t d = 0; d < m.D; ++d) pr[d] = th[d] + m.step[d] * normal_draw(m, c, iter, d);
+        return;
+    }
+    double z1[32];
+    for (uint32_t d = 0; d < m.D; ++d) z1[d] = normal_draw(m, c, iter, 32 + d);
+    for (uint32_t d = 0; d < m.D; ++d) {
+        double lz = 0.0;
+        for (uint32_t k = 0; k <= d; ++k) lz += m.chol[d * m.D + k] * z1[k];
+        pr[d] = th[d] + m.beta * m.step[d] * normal_draw(m, c, iter, d) + (1.0 - m.beta) * lz;
+    }
 }
 
 // log NB(k; size r, mean mu) = lgamma(k+r) - lgamma(r) - lgamma(k+1) + r log(r/(r+mu)) + k log(mu/(r+mu)),
@@ -239,7 +262,7 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     m.k0 = (uint32_t)cfg->seed;
     m.k1 = (uint32_t)(cfg->seed >> 32);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t n_d = al(3 * D * 8), n_y = al((size_t)m.Mo * m.S * 4), n_mr = al((m.Mo + 1) * 4);
+    const size_t n_d = al((3 * D + D * D) * 8), n_y = al((size_t)m.Mo * m.S * 4), n_mr = al((m.Mo + 1) * 4);
     const size_t n_cd = al((size_t)C * D * 8), n_c8 = al((size_t)C * 8), n_cr = al((size_t)C * R * 8);
     const size_t n_c4 = al((size_t)C * 4), n_c1 = al(C), n_ch = al((size_t)m.iters * C * D * 8 + 8);
     const size_t n_fl = al((size_t)m.iters * C + 1), n_refs = al((size_t)C * R * sizeof(SeriesRef));
@@ -258,6 +281,9 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     m.lo = box;
     m.hi = box + D;
     m.step = box + 2 * D;
+    m.chol = box + 3 * D;
+    m.beta = 0.05;
+    m.use_cov = 0;
     m.y = (const uint32_t*)take(n_y);
     m.mrow = (const uint32_t*)take(n_mr);
     m.theta = (double*)take(n_cd);
@@ -335,7 +361,7 @@ int arbo_mcmc_propose(arbo_mcmc* h, uint32_t iter, double* out, void* stream)
     MCUDA(cudaSetDevice(h->device));
     cudaStream_t st = (cudaStream_t)stream;
     const uint32_t n = h->m.C * h->m.D;
-    k_propose<<<(n + 127) / 128, 128, 0, st>>>(h->m, iter);
+    k_propose<<<(h->m.C + 127) / 128, 128, 0, st>>>(h->m, iter);
     MCUDA(cudaGetLastError());
     if (out) {
         MCUDA(cudaMemcpyAsync(out, h->m.prop, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
@@ -421,6 +447,24 @@ int arbo_mcmc_chain(arbo_mcmc* h, uint32_t iters, double* out, uint8_t* flags)
     MCUDA(cudaDeviceSynchronize());
     MCUDA(cudaMemcpy(out, h->m.chain, (size_t)iters * h->m.C * h->m.D * 8, cudaMemcpyDeviceToHost));
     if (flags) MCUDA(cudaMemcpy(flags, h->m.flag, (size_t)iters * h->m.C, cudaMemcpyDeviceToHost));
+    return ARBO_OK;
+}
+
+int arbo_mcmc_set_proposal(arbo_mcmc* h, const double* chol, double beta)
+{
+    if (!h || !(beta >= 0.0 && beta <= 1.0)) return mfail(ARBO_ERR_INVALID, "arbo_mcmc_set_proposal: bad arguments");
+    MCUDA(cudaSetDevice(h->device));
+    MCUDA(cudaDeviceSynchronize());
+    if (!chol) {
+        h->m.use_cov = 0;
+        return ARBO_OK;
+    }
+    const uint32_t D = h->m.D;
+    for (uint32_t i = 0; i < D * D; ++i)
+        if (!std::isfinite(chol[i])) return mfail(ARBO_ERR_INVALID, "arbo_mcmc_set_proposal: non-finite factor");
+    MCUDA(cudaMemcpy((void*)h->m.chol, chol, (size_t)D * D * 8, cudaMemcpyHostToDevice));
+    h->m.beta = beta;
+    h->m.use_cov = 1;
     return ARBO_OK;
 }
 

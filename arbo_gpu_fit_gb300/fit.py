@@ -29,6 +29,16 @@ STEP_FRACTION = 0.01
 # Pseudo-marginal chains, whose likelihood is a noisy estimate, do best well below the 0.234 of
 # exact random-walk Metropolis (Sherlock et al. 2015 give about 0.07 at the optimal noise level).
 TARGET_ACCEPT = [0.234]
+# First iteration of the adaptive-covariance proposal (MCMC::calcCov, cpp/MCMC.cpp:88-161); 0: the
+# diagonal random walk only. A one-element list so the command line can set it.
+COV_START = [0]
+
+
+def adaptation(adapt_until: int) -> "mcmc.Adaptation":
+    """The burn-in adaptation of every arm: the random-walk scale aimed at TARGET_ACCEPT, and from
+    COV_START (when set) the chains' pooled covariance as the proposal, both frozen after adapt_until."""
+    cov = mcmc.CovAdapter(COV_START[0], adapt_until) if COV_START[0] > 0 else None
+    return mcmc.Adaptation(mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]), cov)
 
 
 @dataclass
@@ -83,7 +93,7 @@ def summarize(chain: np.ndarray, minutes: float, burn: int) -> dict:
 
 def run_plain(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
-    r = mcmc.run_plain(m, iters, fs.theta0, adapt=mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]))
+    r = mcmc.run_plain(m, iters, fs.theta0, adapt=adaptation(adapt_until))
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
     out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
@@ -107,7 +117,7 @@ def train_surrogate(fs: FitSetup, runs: int, epochs: int, seed: int = 3, hidden:
 def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
     r = mcmc.run_delayed(m, iters, fs.theta0, lambda th: sur.loglik(th, fs.observed),
-                         adapt=mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]))
+                         adapt=adaptation(adapt_until))
     chain, flags = m.chain(iters)
     accept_per_iter = flags[1:].mean()
     st = m.state()
@@ -121,12 +131,13 @@ def run_delayed(fs: FitSetup, sur: Surrogate, iters: int, seed: int = 1, adapt_u
 
 def run_batched(fs: FitSetup, iters: int, seed: int = 1, adapt_until: int = 0) -> dict:
     m = mcmc.MCMC(fs.workload, fs.observed, fs.chains, fs.step, seed=seed, max_iters=iters, replicates=fs.replicates)
-    adapt = mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0])
+    adapt = adaptation(adapt_until)
     r = mcmc.run_batched(m, iters, fs.theta0, adapt=adapt)
     chain, flags = m.chain(iters)
     out = summarize(chain, r["wall_s"] / 60.0, min(adapt_until + 1, iters - 2))
     out.update(wall_s=r["wall_s"], sim_s=r["sim_s"], simulations=r["simulations"], accept=float(flags[1:].mean()),
-               s_per_iter=r["wall_s"] / iters, chain=chain, flags=flags, schedule=adapt.schedule(fs.step, iters),
+               s_per_iter=r["wall_s"] / iters, chain=chain, flags=flags, schedule=adapt.step.schedule(fs.step, iters),
+               chol=adapt.cov.schedule(len(fs.step), iters) if adapt.cov else np.zeros((iters, len(fs.step), len(fs.step))),
                mcmc_seed=seed)
     m.close()
     return out
@@ -143,7 +154,7 @@ def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt
     time is plain_iters measured iterations scaled to `iters` (every iteration simulates every
     chain once). The first plain_iters states of both are compared here as well."""
     fs = setup(population, chains=chains, seed=seed, step_fraction=step_fraction, replicates=replicates, start=start)
-    out = {"population": population, "start": start, "target_accept": TARGET_ACCEPT[0],
+    out = {"population": population, "start": start, "target_accept": TARGET_ACCEPT[0], "cov_start": COV_START[0],
            "step_fraction": step_fraction, "replicates": replicates,
            "chains": chains, "iters": iters, "adapt_until": adapt_until, "theta_true": THETA_TRUE.tolist()}
     b = run_batched(fs, iters, adapt_until=adapt_until)
@@ -159,11 +170,11 @@ def compare(population: str = "small", chains: int = 64, iters: int = 240, adapt
     if save:
         np.savez_compressed(save, population=population, seed=seed, replicates=replicates, chains=chains,
                             months=fs.months, theta0=fs.theta0, observed=fs.observed, step0=fs.step,
-                            schedule=b["schedule"], mcmc_seed=b["mcmc_seed"], batched_chain=b["chain"],
+                            schedule=b["schedule"], chol=b["chol"], mcmc_seed=b["mcmc_seed"], batched_chain=b["chain"],
                             batched_flags=b["flags"], delayed_chain=d["chain"], adapt_until=adapt_until)
     for r_ in (b, d):
         r_.pop("chain")
-    for k_ in ("flags", "schedule"):
+    for k_ in ("flags", "schedule", "chol"):
         b.pop(k_)
     p.pop("chain")
     out.update(plain=plain, batched=b, delayed=d, surrogate=info)
@@ -228,6 +239,8 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--target-accept", type=float, default=0.234, help="acceptance aimed at during burn-in")
+    ap.add_argument("--cov-start", type=int, default=0,
+                    help="first iteration of the adaptive-covariance proposal (0: diagonal random walk only)")
     ap.add_argument("--start", choices=["near", "spread"], default="near",
                     help="chains start near the true vector or over the middle half of the box")
     ap.add_argument("--save", default=None, help="npz with the chains, data and step schedule (for a serial check)")
@@ -237,6 +250,7 @@ def main(argv=None):
     a = ap.parse_args(argv)
     _native.check(_native.load().arbo_set_device(a.device))
     TARGET_ACCEPT[0] = a.target_accept
+    COV_START[0] = a.cov_start
     if a.time_batch:
         print(json.dumps(time_batch(a.population, a.time_batch, a.time_steps, a.warm_steps)))
         return

@@ -134,6 +134,14 @@ class MCMC:
         self.step_sd = np.ascontiguousarray(step, np.float64)
         check(self._lib.arbo_mcmc_set_step(self._h, _dp(self.step_sd)))
 
+    def set_proposal(self, chol: Optional[np.ndarray], beta: float = 0.05) -> None:
+        """Adaptive-covariance proposals (arbo_mcmc_set_proposal); None: diagonal random walk."""
+        if chol is None:
+            check(self._lib.arbo_mcmc_set_proposal(self._h, None, float(beta)))
+            return
+        L = np.ascontiguousarray(chol, np.float64).reshape(self.D, self.D)
+        check(self._lib.arbo_mcmc_set_proposal(self._h, _dp(L), float(beta)))
+
     def propose(self, it: int) -> np.ndarray:
         out = np.zeros((self.C, self.D), np.float64)
         check(self._lib.arbo_mcmc_propose(self._h, int(it), _dp(out), None))
@@ -267,6 +275,85 @@ class StepAdapter:
         return out
 
 
+class CovAdapter:
+    """Adaptive Metropolis (MCMC::calcCov / propose, cpp/MCMC.cpp:88-161) for many chains: every
+    `every` iterations from `start` to `until`, the covariance of the states of all chains over the
+    second half of the iterations so far, scaled by 2.38^2 / params, becomes the proposal covariance
+    (its Cholesky factor; weight 1 - beta, the diagonal random walk beta). The reference adapts one
+    chain from its own history after 100 * params steps and never stops; here the chains pool
+    their states and adaptation stops at `until`, so the kept iterations form a fixed-proposal
+    Metropolis-Hastings chain."""
+
+    def __init__(self, start: int, until: int, every: int = 10, beta: float = 0.05):
+        self.start, self.until, self.every, self.beta = int(start), int(until), int(every), float(beta)
+        self.chol = None
+        self.set_at = {}  # iteration -> factor in force from that iteration on
+
+    def __call__(self, m: "MCMC", it: int) -> None:
+        if it < self.start or it > self.until or it % self.every:
+            return
+        chain, _ = m.chain(it + 1)
+        x = chain[max(1, (it + 1) // 2):].reshape(-1, m.D)
+        cov = np.cov(x, rowvar=False) * (2.38 ** 2 / m.D)
+        cov += np.eye(m.D) * 1e-12 * max(float(np.trace(cov)) / m.D, 1e-30)
+        try:
+            L = np.linalg.cholesky(cov)
+        except np.linalg.LinAlgError:
+            return
+        self.chol = L
+        self.set_at[it + 1] = L.copy()
+        m.set_proposal(L, self.beta)
+
+    def apply(self, m: "MCMC") -> None:
+        if self.chol is not None:
+            m.set_proposal(self.chol, self.beta)
+
+    def state(self) -> dict:
+        return {"chol": None if self.chol is None else self.chol.tolist(),
+                "set_at": {k: v.tolist() for k, v in self.set_at.items()}}
+
+    def load(self, st: dict) -> None:
+        self.chol = None if st.get("chol") is None else np.asarray(st["chol"], np.float64)
+        self.set_at = {int(k): np.asarray(v, np.float64) for k, v in st.get("set_at", {}).items()}
+
+    def schedule(self, D: int, iters: int) -> np.ndarray:
+        """Proposal factor in force at every iteration, [iters, D, D] (zeros: diagonal walk)."""
+        out = np.zeros((iters, D, D))
+        cur = np.zeros((D, D))
+        for it in range(iters):
+            cur = self.set_at.get(it, cur)
+            out[it] = cur
+        return out
+
+
+class Adaptation:
+    """The burn-in adaptations of a run together (each called after every iteration)."""
+
+    def __init__(self, step: "StepAdapter", cov: Optional[CovAdapter] = None):
+        self.step, self.cov = step, cov
+
+    def __call__(self, m: "MCMC", it: int) -> None:
+        self.step(m, it)
+        if self.cov is not None:
+            self.cov(m, it)
+
+    def apply(self, m: "MCMC") -> None:
+        if self.cov is not None:
+            self.cov.apply(m)
+
+    def state(self) -> dict:
+        return {"step": self.step.state(), "cov": self.cov.state() if self.cov is not None else None}
+
+    def load(self, st: dict) -> None:
+        self.step.load(st.get("step", {}))
+        if self.cov is not None and st.get("cov") is not None:
+            self.cov.load(st["cov"])
+
+    @property
+    def history(self):
+        return self.step.history
+
+
 @dataclass
 class Checkpoint:
     """The state of every chain after iteration `it`: enough for a new MCMC handle to continue the
@@ -325,6 +412,8 @@ def _resume(m: "MCMC", resume: Checkpoint, adapt: Optional["StepAdapter"]) -> in
     m.restore(resume)
     if adapt is not None:
         adapt.load(resume.adapt)
+        if hasattr(adapt, "apply"):
+            adapt.apply(m)  # an adapted proposal covariance lives on the device
     return resume.it + 1
 
 

@@ -509,6 +509,12 @@ int arbo_mcmc_destroy(arbo_mcmc* m);
 int arbo_mcmc_set_state(arbo_mcmc* m, const double* theta, void* stream);
 /* Replaces the random-walk standard deviations (params doubles), e.g. while adapting during burn-in. */
 int arbo_mcmc_set_step(arbo_mcmc* m, const double* step);
+/* The adaptive proposal of MCMC::propose / calcCov (cpp/MCMC.cpp:88-161): chol is the lower
+ * Cholesky factor (params x params, row-major) of 2.38^2 / params times a covariance of the chains'
+ * states; proposals become theta + beta * step * z0 + (1 - beta) * chol * z1 (the reference: beta
+ * 0.05, covariance of one chain's accepted values, used after 100 * params steps). chol = NULL
+ * returns to the diagonal random walk theta + step * z0. */
+int arbo_mcmc_set_proposal(arbo_mcmc* m, const double* chol, double beta);
 /* MCMC::propose (cpp/MCMC.cpp:100-137) without the adaptive covariance: theta + step * N(0, 1)
  * per parameter. out (optional, chains * params) receives the proposals. */
 int arbo_mcmc_propose(arbo_mcmc* m, uint32_t iter, double* out, void* stream);

@@ -107,12 +107,14 @@ def calc_log_likelihood(particles) -> float:
 
 
 def run(workload, observed, chains, step, seed, iters, theta0, replicates=1, nb_size=10.0, box=None,
-        report_param=5, subset=None, threads=1):
+        report_param=5, subset=None, threads=1, chol=None, beta=0.05):
     """Returns (chain[iters, n, D], accepted flags[iters, n], logpost[n]) for the chains in `subset`
     (default: all), n = len(subset). `step` is one vector of random-walk standard deviations or a
     schedule [iters, D] (the burn-in adaptation of a GPU run); theta0 holds every chain's start.
     `threads` > 1 runs the oracle simulations of an iteration in parallel threads (the oracle is C
-    code called through ctypes, which releases the GIL)."""
+    code called through ctypes, which releases the GIL). `chol` [iters, D, D] is the adapted
+    proposal factor in force at each iteration (all zero: the diagonal walk), with weight 1 - beta:
+    proposal = theta + beta * step * z0 + (1 - beta) * chol z1, z1 the draws 32 + d."""
     from concurrent.futures import ThreadPoolExecutor
 
     box = box if box is not None else configs.PRIOR_BOX
@@ -161,11 +163,23 @@ def run(workload, observed, chains, step, seed, iters, theta0, replicates=1, nb_
         flags[0] = True
         for it in range(1, iters):
             props = theta.copy()
+            L = None if chol is None or not np.any(chol[it]) else np.asarray(chol[it], np.float64)
+
+            def normal(c, k):
+                v = _draw(key, STREAM_PROPOSE, c, it, k)
+                return math.sqrt(-2.0 * math.log(u01d(v[0], v[1]))) * math.cos(6.283185307179586 * u01d(v[2], v[3]))
+
             for j, c in enumerate(subset):
+                if L is None:
+                    for d in range(D):
+                        props[j, d] = theta[j][d] + steps[it][d] * normal(c, d)
+                    continue
+                z1 = [normal(c, 32 + d) for d in range(D)]
                 for d in range(D):
-                    v = _draw(key, STREAM_PROPOSE, c, it, d)
-                    z = math.sqrt(-2.0 * math.log(u01d(v[0], v[1]))) * math.cos(6.283185307179586 * u01d(v[2], v[3]))
-                    props[j, d] = theta[j][d] + steps[it][d] * z
+                    lz = 0.0
+                    for k in range(d + 1):
+                        lz += L[d, k] * z1[k]
+                    props[j, d] = theta[j][d] + beta * steps[it][d] * normal(c, d) + (1.0 - beta) * lz
             lls = logliks(props, it)
             for j, c in enumerate(subset):
                 lp = lls[j] if inbox(props[j]) else -math.inf

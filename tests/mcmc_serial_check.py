@@ -35,7 +35,8 @@ def check(path: str, chains: int, iters: int, threads: int, burn: int = 0) -> di
     gpu = z["batched_chain"][:iters, subset]
     t0 = time.perf_counter()
     ser, flags, _ = mcmc_serial.run(w, z["observed"], C, z["schedule"][:iters], int(z["mcmc_seed"]), iters,
-                                    z["theta0"], replicates=int(z["replicates"]), subset=subset, threads=threads)
+                                    z["theta0"], replicates=int(z["replicates"]), subset=subset, threads=threads,
+                                    chol=z["chol"][:iters] if "chol" in z.files else None)
     secs = time.perf_counter() - t0
     rel = np.abs(ser - gpu) / np.maximum(np.abs(ser), 1e-12)
     k = min(burn, iters - 1)

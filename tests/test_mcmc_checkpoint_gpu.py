@@ -17,6 +17,11 @@ pytestmark = pytest.mark.gpu
 ITERS, CUT = 12, 5
 
 
+def adapters():
+    # Scale adaptation and, from iteration 4, the adaptive covariance: both must survive a resume.
+    return mcmc.Adaptation(mcmc.StepAdapter(until=8, every=2), mcmc.CovAdapter(start=3, until=9, every=3))
+
+
 def _screen(th):
     return -50.0 * (th[:, 5] - 0.3) ** 2  # a deterministic first stage
 
@@ -33,7 +38,7 @@ def _run(driver, m, theta0, **kw):
 def test_resumed_chain_equals_uninterrupted(gpu, tmp_path, driver):
     w, obs, theta0 = setup(chains=3)
     full = mcmc.MCMC(w, obs, 3, STEP, seed=31, max_iters=ITERS)
-    ad_full = mcmc.StepAdapter(until=8, every=2)
+    ad_full = adapters()
     _run(driver, full, theta0, iters=ITERS, adapt=ad_full)
     want_chain, want_flags = full.chain(ITERS)
     want = full.state()
@@ -41,14 +46,14 @@ def test_resumed_chain_equals_uninterrupted(gpu, tmp_path, driver):
 
     path = str(tmp_path / "ck.npz")
     first = mcmc.MCMC(w, obs, 3, STEP, seed=31, max_iters=ITERS)
-    ad1 = mcmc.StepAdapter(until=8, every=2)
+    ad1 = adapters()
     _run(driver, first, theta0, iters=CUT + 1, adapt=ad1, on_iter=mcmc.Checkpointer(first, path, CUT, ad1))
     first.close()  # the interruption: nothing of the first handle survives but the file
 
     ck = mcmc.load_checkpoint(path)
     assert ck.it == CUT and ck.chain.shape[0] == CUT + 1
     second = mcmc.MCMC(w, obs, 3, STEP, seed=31, max_iters=ITERS)
-    ad2 = mcmc.StepAdapter(until=8, every=2)
+    ad2 = adapters()
     _run(driver, second, theta0, iters=ITERS, adapt=ad2, resume=ck)
     got_chain, got_flags = second.chain(ITERS)
     got = second.state()
@@ -60,4 +65,5 @@ def test_resumed_chain_equals_uninterrupted(gpu, tmp_path, driver):
     assert np.array_equal(got["accepted"], want["accepted"])
     assert np.array_equal(got["passed"], want["passed"])
     assert ad2.history == ad_full.history
+    assert np.array_equal(ad2.cov.chol, ad_full.cov.chol)
     assert want_flags[1:].any()  # the chains moved

@@ -88,3 +88,21 @@ def test_chain_files(gpu, tmp_path):
     for it in range(1, 5):
         if flags[it, 0]:
             assert np.allclose([float(x) for x in cand[it][2:-1]], chain[it, 0])
+
+
+def test_adaptive_covariance_chain_equals_serial_replay(gpu):
+    # The reference's adaptive proposal (MCMC::calcCov / propose, cpp/MCMC.cpp:88-161): from
+    # iteration 4 the pooled covariance of the chains drives the proposals. The GPU chain must equal
+    # the serial FP64 replay given the same factor schedule.
+    w, obs, theta0 = setup(chains=4)
+    m = mcmc.MCMC(w, obs, 4, STEP, seed=23, max_iters=10)
+    ad = mcmc.Adaptation(mcmc.StepAdapter(0), mcmc.CovAdapter(start=3, until=7, every=2))
+    mcmc.run_batched(m, 10, theta0, adapt=ad)
+    got, flags = m.chain(10)
+    chol = ad.cov.schedule(6, 10)
+    assert np.any(chol[-1])  # the covariance was in use
+    want, wflags, wlp = mcmc_serial.run(w, obs, 4, STEP, 23, 10, theta0, chol=chol)
+    assert np.array_equal(flags, wflags), (flags, wflags)
+    np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(m.state()["logpost"], wlp, rtol=1e-10)
+    m.close()
