@@ -37,7 +37,7 @@ COV_START = [0]
 def adaptation(adapt_until: int) -> "mcmc.Adaptation":
     """The burn-in adaptation of every arm: the random-walk scale aimed at TARGET_ACCEPT, and from
     COV_START (when set) the chains' pooled covariance as the proposal, both frozen after adapt_until."""
-    cov = mcmc.CovAdapter(COV_START[0], adapt_until) if COV_START[0] > 0 else None
+    cov = mcmc.CovAdapter(COV_START[0], adapt_until, target=TARGET_ACCEPT[0]) if COV_START[0] > 0 else None
     return mcmc.Adaptation(mcmc.StepAdapter(adapt_until, target=TARGET_ACCEPT[0]), cov)
 
 

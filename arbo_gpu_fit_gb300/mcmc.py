@@ -282,19 +282,31 @@ class CovAdapter:
     (its Cholesky factor; weight 1 - beta, the diagonal random walk beta). The reference adapts one
     chain from its own history after 100 * params steps and never stops; here the chains pool
     their states and adaptation stops at `until`, so the kept iterations form a fixed-proposal
-    Metropolis-Hastings chain."""
+    Metropolis-Hastings chain. With `target`, a global scale of the covariance follows the
+    acceptance of each block (a noisy, pseudo-marginal likelihood accepts far less than the 0.234 the
+    2.38^2/params scale is tuned for)."""
 
-    def __init__(self, start: int, until: int, every: int = 10, beta: float = 0.05):
+    def __init__(self, start: int, until: int, every: int = 10, beta: float = 0.05, target: Optional[float] = None):
         self.start, self.until, self.every, self.beta = int(start), int(until), int(every), float(beta)
+        self.target = target  # acceptance aimed at by a global scale of the covariance (None: fixed 2.38^2/params)
+        self.lam = 1.0
+        self.last = None
         self.chol = None
         self.set_at = {}  # iteration -> factor in force from that iteration on
 
     def __call__(self, m: "MCMC", it: int) -> None:
         if it < self.start or it > self.until or it % self.every:
             return
+        if self.target is not None:
+            # Adaptive scaling (Andrieu & Thoms 2008): the acceptance of the last block moves the scale.
+            acc = int(m.state()["accepted"].sum())
+            if self.last is not None and self.chol is not None:
+                rate = (acc - self.last) / float(m.C * self.every)
+                self.lam *= float(np.clip(np.exp(2.0 * (rate - self.target)), 0.5, 2.0))
+            self.last = acc
         chain, _ = m.chain(it + 1)
         x = chain[max(1, (it + 1) // 2):].reshape(-1, m.D)
-        cov = np.cov(x, rowvar=False) * (2.38 ** 2 / m.D)
+        cov = np.cov(x, rowvar=False) * (2.38 ** 2 / m.D) * self.lam ** 2
         cov += np.eye(m.D) * 1e-12 * max(float(np.trace(cov)) / m.D, 1e-30)
         try:
             L = np.linalg.cholesky(cov)
@@ -309,10 +321,12 @@ class CovAdapter:
             m.set_proposal(self.chol, self.beta)
 
     def state(self) -> dict:
-        return {"chol": None if self.chol is None else self.chol.tolist(),
+        return {"chol": None if self.chol is None else self.chol.tolist(), "lam": self.lam, "last": self.last,
                 "set_at": {k: v.tolist() for k, v in self.set_at.items()}}
 
     def load(self, st: dict) -> None:
+        self.lam = float(st.get("lam", 1.0))
+        self.last = st.get("last")
         self.chol = None if st.get("chol") is None else np.asarray(st["chol"], np.float64)
         self.set_at = {int(k): np.asarray(v, np.float64) for k, v in st.get("set_at", {}).items()}
 

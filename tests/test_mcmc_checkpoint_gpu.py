@@ -19,7 +19,7 @@ ITERS, CUT = 12, 5
 
 def adapters():
     # Scale adaptation and, from iteration 4, the adaptive covariance: both must survive a resume.
-    return mcmc.Adaptation(mcmc.StepAdapter(until=8, every=2), mcmc.CovAdapter(start=3, until=9, every=3))
+    return mcmc.Adaptation(mcmc.StepAdapter(until=8, every=2), mcmc.CovAdapter(start=3, until=9, every=3, target=0.2))
 
 
 def _screen(th):
