@@ -47,8 +47,8 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # Per-launch DRAM traffic of the demographic kernel on this workload, from one ncu capture of a
 # launch at step 5 (the command is kept with its summary under profiles/):
-# dram__bytes_read.sum + dram__bytes_write.sum (42,423,296 + 7,979,008 bytes).
-DEMOG_TRAFFIC_BYTES = 50_402_304
+# dram__bytes_read.sum + dram__bytes_write.sum (42,415,616 + 7,958,272 bytes).
+DEMOG_TRAFFIC_BYTES = 50_373_888
 
 
 def parse():
