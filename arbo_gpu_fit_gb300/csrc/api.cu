@@ -1398,6 +1398,13 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     b->blocks[1] = foi_off[n];
     b->blocks[2] = infect_off[n];
     bd.grid_demog = std::max(1u, std::min(b->blocks[0], l.numSM * occ[0]));
+    // Demographic items per counter fetch: 4, then single items once fewer than 8 per resident
+    // warp are left (the last fetches set the end of the pass). Against pairs throughout: demographic
+    // phase 2.50 -> 2.42 ms on the 256 uneven instances, 1.49 -> 1.45 ms on 64 config-1 instances,
+    // 184 -> 178 us on 512 instances of 7e4 agents; single items throughout were slower on all three
+    // (more fetches of one counter).
+    bd.demog_chunk = 4u;
+    bd.demog_tail = 8u * bd.grid_demog * (l.demogBlock / 32);
     // Force of infection: one item per run. Longer runs left a few warps with the heavy pairs of
     // large instances (phase 0.29 against 0.12 ms on the 256 large instances; the same on small ones).
     bd.foi_run = 1;

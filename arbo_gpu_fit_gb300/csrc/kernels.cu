@@ -1134,10 +1134,11 @@ __device__ __forceinline__ void batch_warp_items(const BatchDev& bd, const uint3
 
 // Demographic pass of a batch. Work items are per warp: 32*U-lane groups of humans or one
 // mosquito quad, instance by instance (bd.demog_off counts warp items, bd.demog_h the human items
-// of each instance). Warps take pairs of consecutive items from a device counter (reset by the
-// force-of-infection kernel once this kernel has finished), so uneven instances balance across
-// the GPU, and each warp keeps a private copy of its current instance's descriptor in shared
-// memory: no block-wide barrier anywhere.
+// of each instance). Warps take runs of bd.demog_chunk consecutive items from a device counter
+// (reset by the force-of-infection kernel once this kernel has finished), single items once fewer
+// than bd.demog_tail are left, so uneven instances balance across the GPU, and each warp keeps a
+// private copy of its current instance's descriptor in shared memory: no block-wide barrier
+// anywhere.
 template <int U>
 __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t koff)
 {
@@ -1147,12 +1148,15 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
     const Dev& d = *reinterpret_cast<const Dev*>(wdev[warp]);
     const uint32_t total = __ldg(&bd.demog_off[bd.n]);
     uint32_t inst = UINT_MAX, lo = 0, hi = 0;  // current instance and its item range
+    uint32_t chunk = bd.demog_chunk;
     for (;;) {
         uint32_t it0 = 0;
-        if (lane == 0) it0 = atomicAdd(bd.work, 2u);
+        if (lane == 0) it0 = atomicAdd(bd.work, chunk);
         it0 = __shfl_sync(kFull, it0, 0);
         if (it0 >= total) break;
-        for (uint32_t it = it0; it < it0 + 2 && it < total; ++it) {
+        const uint32_t end = min(it0 + chunk, total);
+        if (total - end < bd.demog_tail) chunk = 1u;
+        for (uint32_t it = it0; it < end; ++it) {
             if (inst == UINT_MAX || it >= hi) {
                 // Items arrive in increasing order: usually the next instance, else search.
                 const bool next = inst != UINT_MAX && inst + 2 <= bd.n && it < __ldg(&bd.demog_off[inst + 2]);

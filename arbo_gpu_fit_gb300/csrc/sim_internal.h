@@ -146,6 +146,8 @@ struct BatchDev {
     const uint32_t* infect_off;  // [n+1] communities (the infection kernel runs one warp per community)
     uint32_t n;
     uint32_t grid_demog, grid_foi, grid_infect;  // resident CTAs of each persistent kernel
+    uint32_t demog_chunk;                        // demographic items a warp takes per counter fetch
+    uint32_t demog_tail;                         // below this many items left, one item per fetch
     uint32_t infect_run;                         // consecutive communities per warp run (1..kInfectRunMax)
     uint32_t foi_run;                            // consecutive force-of-infection items per warp run
 };
