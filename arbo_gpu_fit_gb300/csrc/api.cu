@@ -6,8 +6,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/arbo.h"
@@ -110,6 +112,12 @@ uint32_t comm_of_host(const std::vector<uint32_t>& loc, uint32_t P, uint32_t i)
     return lo;
 }
 
+// Death-age tables of one species: CDF per integer age and the inverse bucket table.
+struct AgeTables {
+    std::vector<float> cdf;
+    std::vector<uint32_t> inv;
+};
+
 }  // namespace
 
 struct arbo_sim {
@@ -140,9 +148,10 @@ struct arbo_sim {
     // handle's device (null when the handle exceeds its size or the lookup failed).
     unsigned long long* noalloc = nullptr;
     int noalloc_err = 0;  // cudaError_t of a failed set-up
-    // Fingerprints of the read-only death-age tables (CDF and inverse bucket table), human and
-    // mosquito: handles of one batch with equal tables share one copy in its descriptors.
-    uint64_t tab_h = 0, tab_m = 0;
+    // Host copies of the read-only death-age tables (CDF per integer age and inverse bucket
+    // table), human and mosquito, interned across handles: handles whose tables are equal byte
+    // for byte hold the same object, and a batch gives them one device copy in its descriptors.
+    std::shared_ptr<const AgeTables> tab_h, tab_m;
 };
 
 extern "C" {
@@ -314,7 +323,7 @@ static const char* param_error(const arbo_sim_param& p, uint32_t N, uint32_t M)
     return nullptr;
 }
 
-// FNV-1a fingerprint of a table's bytes and length.
+// FNV-1a fingerprint of a table's bytes and length (the key of the intern table below).
 static uint64_t table_fingerprint(const void* a, size_t na, const void* b, size_t nb)
 {
     uint64_t h = 1469598103934665603ull;
@@ -326,6 +335,34 @@ static uint64_t table_fingerprint(const void* a, size_t na, const void* b, size_
     mix(a, na);
     mix(b, nb);
     return h;
+}
+
+// Interned death-age tables: live AgeTables objects by fingerprint. A lookup returns the object
+// whose bytes equal the given tables (compared in full, so a fingerprint collision only costs a
+// comparison) or makes a new one; entries of released objects are dropped as they are met.
+static std::mutex g_tables_mu;
+static std::unordered_multimap<uint64_t, std::weak_ptr<const AgeTables>> g_tables;
+
+static std::shared_ptr<const AgeTables> intern_tables(const std::vector<float>& cdf, const std::vector<uint32_t>& inv)
+{
+    const uint64_t h = table_fingerprint(cdf.data(), cdf.size() * 4, inv.data(), inv.size() * 4);
+    std::lock_guard<std::mutex> lk(g_tables_mu);
+    auto range = g_tables.equal_range(h);
+    for (auto it = range.first; it != range.second;) {
+        std::shared_ptr<const AgeTables> t = it->second.lock();
+        if (!t) {
+            it = g_tables.erase(it);
+            continue;
+        }
+        if (t->cdf.size() == cdf.size() && t->inv.size() == inv.size() &&
+            std::memcmp(t->cdf.data(), cdf.data(), cdf.size() * 4) == 0 &&
+            std::memcmp(t->inv.data(), inv.data(), inv.size() * 4) == 0)
+            return t;
+        ++it;
+    }
+    auto t = std::make_shared<const AgeTables>(AgeTables{cdf, inv});
+    g_tables.emplace(h, t);
+    return t;
 }
 
 int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const arbo_io_param* io, const arbo_csr* csr,
@@ -504,8 +541,8 @@ int arbo_sim_create(const arbo_sim_param* sp, const arbo_arch_param* ap, const a
     UP(d.tcomm, tcomm.data(), (size_t)d.tiles * 4);
     UP(d.csr_loc, csr->loc, (P + 1) * 4);
     if (csr->nnz) UP(d.csr_to, csr->to, (size_t)csr->nnz * 4);
-    s->tab_h = table_fingerprint(cdfh.data(), cdfh.size() * 4, minvh.data(), minvh.size() * 4);
-    s->tab_m = table_fingerprint(cdfm.data(), cdfm.size() * 4, minv.data(), minv.size() * 4);
+    s->tab_h = intern_tables(cdfh, minvh);
+    s->tab_m = intern_tables(cdfm, minv);
     UP(d.cdfh, cdfh.data(), cdfh.size() * 4);
     UP(d.cdfm, cdfm.data(), cdfm.size() * 4);
     UP(d.minv, minv.data(), minv.size() * 4);
@@ -1315,8 +1352,8 @@ void batch_share_tables(arbo_batch* b)
         for (size_t j = 0; j < i; ++j) {
             const arbo_sim* o = b->sims[j];
             if (o->device != s->device) continue;
-            if (b->tab_owner_h[i] == i && o->tab_h == s->tab_h && o->d.ah == s->d.ah) b->tab_owner_h[i] = (uint32_t)j;
-            if (b->tab_owner_m[i] == i && o->tab_m == s->tab_m && o->d.am == s->d.am) b->tab_owner_m[i] = (uint32_t)j;
+            if (b->tab_owner_h[i] == i && o->tab_h == s->tab_h) b->tab_owner_h[i] = (uint32_t)j;
+            if (b->tab_owner_m[i] == i && o->tab_m == s->tab_m) b->tab_owner_m[i] = (uint32_t)j;
         }
     }
 }

@@ -1,7 +1,8 @@
 """Batched stepping (arbo_batch_*): many instances of uneven sizes and parameters advanced by one
 persistent kernel per phase must give, instance for instance, the same census, counters and
 series as stepping each handle alone (bit for bit), for every launch shape and across the
-autotuner's shape changes; one instance is also checked against the serial oracle."""
+autotuner's shape changes, whether an instance's death-age tables are shared with others or its
+own; one instance is also checked against the serial oracle."""
 import numpy as np
 import pytest
 
@@ -21,6 +22,10 @@ def workloads(T=40):
         sp.bitingRate, sp.externalInfection = 0.9, 8.0
         sp.nInitialInf, sp.mInitialInf = float(max(int(sp.nSize) // 30, 1)), float(max(int(sp.mSize) // 30, 1))
     ws.append(small_case(T=T))
+    # Two instances with life expectancies of their own: their death-age tables differ from the
+    # others', which the batch gives one shared device copy.
+    ws[1].parameter.simulation.mScaleLifeExpectancy *= 1.25
+    ws[3].parameter.simulation.nScaleLifeExpectancy *= 0.8
     return ws
 
 
