@@ -47,8 +47,8 @@ PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # Per-launch DRAM traffic of the demographic kernel on this workload, from one ncu capture of a
 # launch at step 5 (the command is kept with its summary under profiles/):
-# dram__bytes_read.sum + dram__bytes_write.sum (42,415,616 + 7,958,272 bytes).
-DEMOG_TRAFFIC_BYTES = 50_373_888
+# dram__bytes_read.sum + dram__bytes_write.sum (42,747,136 + 8,205,824 bytes).
+DEMOG_TRAFFIC_BYTES = 50_952_960
 
 
 def parse():
