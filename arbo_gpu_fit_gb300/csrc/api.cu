@@ -1311,6 +1311,7 @@ struct arbo_batch {
     BatchDev bd{};
     void* mem = nullptr;  // Dev[n] followed by the four offset tables
     uint32_t blocks[3] = {0, 0, 0};
+    uint32_t init_blocks[4] = {0, 0, 0, 0};  // grids of the batched initialisation kernels
     cudaStream_t cap = nullptr;
     cudaGraphExec_t gmulti = nullptr, gone = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1386,9 +1387,25 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     l.numSM = a.totalSM ? a.totalSM : 152u;
     l.pdl = 1;
     std::vector<uint32_t> demog_off(n + 1, 0), demog_h(n, 0), foi_off(n + 1, 0), infect_off(n + 1, 0);
+    std::vector<uint32_t> init_off[4];
+    for (auto& v : init_off) v.assign(n + 1, 0);
     const uint32_t K = a.infectBlock / 32;  // communities (warps) per infection CTA
     for (uint32_t i = 0; i < n; ++i) {
         const Dev& d = b->sims[i]->d;
+        // Initialisation blocks of 256 threads (at least one per instance and kernel): humans,
+        // mosquito tiles (eight per block), seeds (thread 0 also resets the step control), and the
+        // reset of counters and series (about eight elements per thread of the longest array).
+        const uint64_t SP = (uint64_t)d.S * d.P, R = (uint64_t)d.T + 1;
+        const uint64_t reset_len = std::max({SP, R * d.S, (uint64_t)d.P, d.recordSpatial ? R * SP : (uint64_t)0});
+        const uint64_t ik[4] = {std::max<uint64_t>(1, cdiv((uint64_t)d.nvec * 4, 256)),
+                                std::max<uint64_t>(1, cdiv(d.tiles, 8)),
+                                std::max<uint64_t>(1, cdiv(std::max(d.nInit, d.mInit), 256)),
+                                std::max<uint64_t>(1, std::min<uint64_t>(cdiv(reset_len, 2048), 4096))};
+        for (int k = 0; k < 4; ++k) {
+            if (init_off[k][i] + ik[k] >= (1ull << 31))
+                return fail(ARBO_ERR_INVALID, "batch too large: more than 2^31 blocks in one phase");
+            init_off[k][i + 1] = init_off[k][i] + (uint32_t)ik[k];
+        }
         const uint64_t hb = cdiv(d.nvec, (uint64_t)32 * a.demogUnroll);  // warp items
         const uint64_t mb = cdiv(d.tiles, kQuad);
         const uint64_t fb = cdiv((uint64_t)d.S * d.P, 32);  // force of infection: warps of 32 pairs
@@ -1404,7 +1421,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     uint32_t occ[3] = {1, 1, 1};
     const int oe = batch_blocks_per_sm(l, occ);
     if (oe) return fail(ARBO_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString((cudaError_t)oe));
-    const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3 + 1) * 4;
+    const size_t devb = align256(sizeof(Dev) * n), tab = (size_t)(4 * n + 3 + 1 + 4 * (n + 1)) * 4;
     if (!b->mem) CUDA_TRY(cudaMalloc(&b->mem, devb + tab));
     std::vector<Dev> devs(n);
     b->versions.resize(n);
@@ -1420,6 +1437,7 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     t.insert(t.end(), foi_off.begin(), foi_off.end());
     t.insert(t.end(), infect_off.begin(), infect_off.end());
     t.push_back(0u);  // demographic work counter
+    for (auto& v : init_off) t.insert(t.end(), v.begin(), v.end());
     CUDA_TRY(cudaMemcpy(b->mem, devs.data(), sizeof(Dev) * n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy((char*)b->mem + devb, t.data(), tab, cudaMemcpyHostToDevice));
     uint32_t* tp = (uint32_t*)((char*)b->mem + devb);
@@ -1430,6 +1448,10 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
     bd.foi_off = tp + (2 * n + 1);
     bd.infect_off = tp + (3 * n + 2);
     bd.work = tp + (4 * n + 3);
+    for (uint32_t k = 0; k < 4; ++k) {
+        bd.init_off[k] = tp + (4 * n + 4) + k * (n + 1);
+        b->init_blocks[k] = init_off[k][n];
+    }
     bd.n = n;
     b->blocks[0] = demog_off[n];
     b->blocks[1] = foi_off[n];
@@ -1636,12 +1658,20 @@ int arbo_batch_get_arch(const arbo_batch* b, arbo_arch_param* arch, uint32_t gri
     return ARBO_OK;
 }
 
+// arbo_sim_init of every instance, in five launches for the whole batch (the same per-agent code;
+// the descriptors are refreshed first, so parameters changed since the last step are used).
 int arbo_batch_init(arbo_batch* b, void* stream)
 {
     if (!b) return fail(ARBO_ERR_INVALID, "null batch");
+    CUDA_TRY(cudaSetDevice(b->device));
+    const int re = batch_refresh(b);
+    if (re) return re;
+    const int e = launch_init_batch(b->bd, b->l, stream, b->init_blocks);
+    if (e) return fail(ARBO_ERR_CUDA, std::string("batch init launch: ") + cudaGetErrorString((cudaError_t)e));
     for (arbo_sim* s : b->sims) {
-        const int e = arbo_sim_init(s, stream);
-        if (e) return e;
+        noalloc_prepare(s);
+        s->host_t = 0;
+        s->inited = true;
     }
     return ARBO_OK;
 }

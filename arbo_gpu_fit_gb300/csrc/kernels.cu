@@ -1180,7 +1180,7 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
 
 // Force-of-infection pass of a batch: one warp per 32 consecutive (serotype, community) pairs of
 // an instance (bd.foi_off counts these warp items), in runs of bd.foi_run items per warp.
-__global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
+__global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, int collect_only, uint32_t koff)
 {
     extern __shared__ __align__(16) unsigned char foi_dyn[];
     const uint32_t warp = threadIdx.x >> 5, W = blockDim.x >> 5;
@@ -1193,7 +1193,7 @@ __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, uint32_t koff)
     }
     griddep_launch_dependents();  // the infection kernel may be scheduled; it waits for this grid
     batch_warp_items(bd, bd.foi_off, bd.foi_run, wdev,
-                     [&](const Dev& d, uint32_t item) { foi_warp(d, 32 * item, 0, koff, sh); });
+                     [&](const Dev& d, uint32_t item) { foi_warp(d, 32 * item, collect_only, koff, sh); });
 }
 
 // Infection pass of a batch: one warp per community over the concatenated communities of all
@@ -1237,11 +1237,8 @@ __global__ void k_advance_batch(BatchDev bd, uint32_t n)
 // ------------------------------------------------------------------ initialisation
 
 // nDemographicInitialization (cpp/demographicintial.cu:86-180), one thread per human slot.
-__global__ void k_init_humans(Dev d)
+__device__ __forceinline__ void init_human(const Dev& d, const Key& key, uint32_t j)
 {
-    const Key key = load_key(d.ctrl);
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= d.nvec * 4) return;
     if (j >= d.N) {
         d.n_status[j] = kPad;
         d.n_born[j] = 0;
@@ -1279,14 +1276,17 @@ __global__ void k_init_humans(Dev d)
     d.n_recovery[j] = 0;
 }
 
-// mDemographicInitialization (cpp/demographicintial.cu:183-297): one warp per 128-slot tile;
-// the tile's dead count starts the carried count of the recruitment quota.
-__global__ void k_init_mosquitoes(Dev d)
+__global__ void k_init_humans(Dev d)
 {
     const Key key = load_key(d.ctrl);
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (b >= d.tiles) return;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < d.nvec * 4) init_human(d, key, j);
+}
+
+// mDemographicInitialization (cpp/demographicintial.cu:183-297): one warp per 128-slot tile;
+// the tile's dead count starts the carried count of the recruitment quota.
+__device__ __forceinline__ void init_mosquito_tile(const Dev& d, const Key& key, uint32_t b, uint32_t lane)
+{
     const float alive_p = __fdiv_rn(__ldg(&d.etab[0]), (float)d.M);
     const uint32_t c0 = __ldg(&d.tcomm[b]);
     uint32_t ndead = 0, ndead0 = 0;  // dead slots of the tile; of them, in the tile's first community
@@ -1334,12 +1334,17 @@ __global__ void k_init_mosquitoes(Dev d)
     }
 }
 
-// nEpidemicInitial / mEpidemicInitial (cpp/epidemicinitial.cu:27-99): the seeded agents are
-// elements 0..k-1 of a keyed bijection of the census. Block 0 also resets the step control.
-__global__ void k_seed(Dev d)
+__global__ void k_init_mosquitoes(Dev d)
 {
     const Key key = load_key(d.ctrl);
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b < d.tiles) init_mosquito_tile(d, key, b, threadIdx.x & 31u);  // warp-uniform
+}
+
+// nEpidemicInitial / mEpidemicInitial (cpp/epidemicinitial.cu:27-99): the seeded agents are
+// elements 0..k-1 of a keyed bijection of the census. Thread 0 also resets the step control.
+__device__ __forceinline__ void seed_one(const Dev& d, const Key& key, uint32_t j)
+{
     if (j == 0) {
         d.ctrl->t = 0;
         d.ctrl->err = 0;
@@ -1373,6 +1378,92 @@ __global__ void k_seed(Dev d)
         d.m_strain[i] = (uint8_t)s;
         atomicAdd(&d.infm[s * d.P + comm_of(d.mloc, d.P, i)], 1u);
     }
+}
+
+__global__ void k_seed(Dev d)
+{
+    const Key key = load_key(d.ctrl);
+    seed_one(d, key, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ------------------------------------------------------------------ batched initialisation
+//
+// arbo_sim_init of every instance of a batch in five launches: the same per-agent bodies, with
+// the blocks of all instances concatenated (off[i] = first block of instance i, every instance
+// at least one block) and each block's instance descriptor staged in shared memory.
+
+// Instance of block blockIdx.x and its first block; the descriptor copied into `buf` by the block.
+__device__ __forceinline__ const Dev& stage_block_desc(const BatchDev& bd, const uint32_t* __restrict__ off,
+                                                       uint32_t& inst, uint32_t& first, unsigned long long* buf)
+{
+    inst = batch_instance(off, bd.n, blockIdx.x);
+    first = __ldg(&off[inst]);
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(bd.devs + inst);
+    for (uint32_t i = threadIdx.x; i < sizeof(Dev) / 8; i += blockDim.x) buf[i] = src[i];
+    __syncthreads();
+    return *reinterpret_cast<const Dev*>(buf);
+}
+
+// The cudaMemsetAsync / cudaMemcpyAsync calls of arbo_sim_init: counters, event counts and
+// series zeroed, each community's alive mosquito count restarted from its slot count. The blocks
+// of one instance stride over its arrays.
+__global__ void __launch_bounds__(256) k_reset_batch(BatchDev bd)
+{
+    __shared__ __align__(16) unsigned long long buf[sizeof(Dev) / 8];
+    uint32_t inst, first;
+    const Dev& d = stage_block_desc(bd, bd.init_off[3], inst, first, buf);
+    const uint32_t nb = __ldg(&bd.init_off[3][inst + 1]) - first;
+    const uint32_t i0 = (blockIdx.x - first) * blockDim.x + threadIdx.x, stride = nb * blockDim.x;
+    const uint32_t SP = d.S * d.P, R = d.T + 1, RS = R * d.S;
+    for (uint32_t i = i0; i < SP; i += stride) {
+        d.infh[i] = 0u;
+        d.infm[i] = 0u;
+        d.inc[i] = 0u;
+        d.transh[i] = 0u;
+        d.transm[i] = 0u;
+    }
+    for (uint32_t i = i0; i < RS; i += stride) {
+        d.s_ninc[i] = 0u;
+        d.s_ninf[i] = 0u;
+        d.s_one[i] = 0u;
+        d.s_minf[i] = 0u;
+    }
+    for (uint32_t i = i0; i < R; i += stride) {
+        d.s_ncount[i] = 0u;
+        d.s_mcount[i] = 0u;
+    }
+    if (d.s_spatial)
+        for (size_t i = i0; i < (size_t)R * SP; i += stride) d.s_spatial[i] = 0u;
+    for (uint32_t i = i0; i < d.P; i += stride) d.mcnt[i] = d.msize[i];
+}
+
+__global__ void __launch_bounds__(256) k_init_humans_batch(BatchDev bd)
+{
+    __shared__ __align__(16) unsigned long long buf[sizeof(Dev) / 8];
+    uint32_t inst, first;
+    const Dev& d = stage_block_desc(bd, bd.init_off[0], inst, first, buf);
+    const Key key = load_key(d.ctrl);
+    const uint32_t j = (blockIdx.x - first) * blockDim.x + threadIdx.x;
+    if (j < d.nvec * 4) init_human(d, key, j);
+}
+
+__global__ void __launch_bounds__(256) k_init_mosquitoes_batch(BatchDev bd)
+{
+    __shared__ __align__(16) unsigned long long buf[sizeof(Dev) / 8];
+    uint32_t inst, first;
+    const Dev& d = stage_block_desc(bd, bd.init_off[1], inst, first, buf);
+    const Key key = load_key(d.ctrl);
+    const uint32_t b = (blockIdx.x - first) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (b < d.tiles) init_mosquito_tile(d, key, b, threadIdx.x & 31u);  // warp-uniform
+}
+
+__global__ void __launch_bounds__(256) k_seed_batch(BatchDev bd)
+{
+    __shared__ __align__(16) unsigned long long buf[sizeof(Dev) / 8];
+    uint32_t inst, first;
+    const Dev& d = stage_block_desc(bd, bd.init_off[2], inst, first, buf);
+    const Key key = load_key(d.ctrl);
+    seed_one(d, key, (blockIdx.x - first) * blockDim.x + threadIdx.x);
 }
 
 
@@ -1623,7 +1714,7 @@ int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* e
     if ((e = (int)cudaGetLastError())) return e;
     if (ev) cudaEventRecord(ev[1], st);
     if ((e = launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), foi_smem(l.foiBlock, true), st, l.pdl != 0, bd,
-                        koff)))
+                        0, koff)))
         return e;
     if (ev) cudaEventRecord(ev[2], st);
     if ((e = launch_pdl(k_infect_batch, dim3(bd.grid_infect), dim3(l.infectBlock), infect_smem(l.infectBlock, true), st,
@@ -1631,6 +1722,20 @@ int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* e
         return e;
     if (ev) cudaEventRecord(ev[3], st);
     return 0;
+}
+
+int launch_init_batch(const BatchDev& bd, const Launch& l, void* stream, const uint32_t blocks[4])
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    k_reset_batch<<<blocks[3], 256, 0, st>>>(bd);
+    k_init_humans_batch<<<blocks[0], 256, 0, st>>>(bd);
+    k_init_mosquitoes_batch<<<blocks[1], 256, 0, st>>>(bd);
+    k_seed_batch<<<blocks[2], 256, 0, st>>>(bd);
+    const int e = (int)cudaGetLastError();
+    if (e) return e;
+    // Series row 0 of every instance (the collect-only pass of arbo_sim_init).
+    return launch_pdl(k_foi_batch, dim3(bd.grid_foi), dim3(l.foiBlock), foi_smem(l.foiBlock, true), st, false, bd, 1,
+                      0u);
 }
 
 int launch_advance_batch(const BatchDev& bd, uint32_t n, void* stream)

@@ -144,6 +144,8 @@ struct BatchDev {
     uint32_t* work;              // demographic item counter (zero between steps)
     const uint32_t* foi_off;     // [n+1] force-of-infection warp items (32 (serotype, community) pairs each)
     const uint32_t* infect_off;  // [n+1] communities (the infection kernel runs one warp per community)
+    const uint32_t* init_off[4];  // [n+1] each: 256-thread blocks of the batched initialisation kernels
+                                  // (humans, mosquito tiles, seeds, counter and series reset)
     uint32_t n;
     uint32_t grid_demog, grid_foi, grid_infect;  // resident CTAs of each persistent kernel
     uint32_t demog_chunk;                        // demographic items a warp takes per counter fetch
@@ -180,6 +182,9 @@ int preload_step_kernels(const Launch& l);
 // Batched steps (see BatchDev); the block shapes come from l, the grids from bd.
 int launch_step_batch(const BatchDev& bd, const Launch& l, void* stream, void* events, uint32_t koff);
 int launch_advance_batch(const BatchDev& bd, uint32_t n, void* stream);
+// arbo_sim_init of every instance: reset, humans, mosquitoes, seeds, series row 0; blocks[k] is the
+// block count of init_off[k].
+int launch_init_batch(const BatchDev& bd, const Launch& l, void* stream, const uint32_t blocks[4]);
 // Records the message returned by arbo_last_error (api.cu) and returns code.
 int set_error(int code, const std::string& msg);
 

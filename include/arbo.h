@@ -437,7 +437,8 @@ int arbo_batch_create(arbo_sim* const* sims, uint32_t n, const arbo_arch_param* 
 int arbo_batch_destroy(arbo_batch* b);
 /* Number of instances and their total agents (humans + mosquito slots). */
 int arbo_batch_size(const arbo_batch* b, uint32_t* n, uint64_t* agents);
-/* arbo_sim_init of every instance. */
+/* arbo_sim_init of every instance, with the parameters and seeds the handles hold now; the same
+ * results as initialising each alone, in five kernel launches for the whole batch. */
 int arbo_batch_init(arbo_batch* b, void* stream);
 /* Advances every instance by nsteps (clamped to the shortest remaining run). */
 int arbo_batch_step(arbo_batch* b, uint32_t nsteps, void* stream);

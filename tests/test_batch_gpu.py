@@ -1,8 +1,11 @@
-"""Batched stepping (arbo_batch_*): many instances of uneven sizes and parameters advanced by one
-persistent kernel per phase must give, instance for instance, the same census, counters and
-series as stepping each handle alone (bit for bit), for every launch shape and across the
+"""Batched initialisation and stepping (arbo_batch_*): many instances of uneven sizes and parameters
+initialised together and advanced by one persistent kernel per phase must give, instance for
+instance, the same census, counters and series as initialising and stepping each handle alone
+(bit for bit), after new parameters and seeds as well, for every launch shape and across the
 autotuner's shape changes, whether an instance's death-age tables are shared with others or its
 own; one instance is also checked against the serial oracle."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -54,6 +57,8 @@ def test_batch_equals_individual_steps(gpu, shape):
     arch = ArchitectureParam(0, **shape) if shape else None
     with Batch(together, arch) as b:
         b.init()
+        for i, (x, y) in enumerate(zip(alone, together)):
+            same(x, y, f"instance {i} after init")
         for k in [1, 6, 13, 20]:
             b.step(k)
             for s in alone:
@@ -61,6 +66,34 @@ def test_batch_equals_individual_steps(gpu, shape):
             for i, (x, y) in enumerate(zip(alone, together)):
                 same(x, y, f"instance {i} at t={x.status()[1]}")
     assert sum(int(s.series("n_incidence").sum()) for s in together) > 0
+
+
+def test_batch_reinit_equals_individual(gpu):
+    # The batched initialisation after a run: new parameters and seeds (as an MCMC iteration sets
+    # them), counters and series of the previous run cleared, every instance as if initialised alone.
+    lib = _native.load()
+    ws = workloads()
+    alone, together = make(ws), make(ws)
+    with Batch(together) as b:
+        for run in range(3):
+            if run:
+                for k, (x, y, w) in enumerate(zip(alone, together, ws)):
+                    sp = w.parameter.simulation.copy()
+                    sp.bitingRate = sp.bitingRate * (0.8 if run == 1 else 1.1)
+                    sp.externalInfection = sp.externalInfection * 0.5 * run
+                    for sim in (x, y):
+                        _native.check(lib.arbo_sim_set_param(sim._h, ctypes.byref(sp)))
+                        sim.set_seed(1000 * run + k, k)
+            for s in alone:
+                s.init()
+            b.init()
+            for i, (x, y) in enumerate(zip(alone, together)):
+                same(x, y, f"run {run}, instance {i} after init")
+            for s in alone:
+                s.step(9)
+            b.step(9)
+            for i, (x, y) in enumerate(zip(alone, together)):
+                same(x, y, f"run {run}, instance {i} after 9 steps")
 
 
 def test_batch_instance_equals_oracle(gpu):
