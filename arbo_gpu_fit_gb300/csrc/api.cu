@@ -1309,7 +1309,7 @@ struct arbo_batch {
     arbo_arch_param arch{};
     Launch l{};
     BatchDev bd{};
-    void* mem = nullptr;  // Dev[n] followed by the four offset tables
+    void* mem = nullptr;  // Dev[n], then the phases' block tables, the work counter, the init block tables
     uint32_t blocks[3] = {0, 0, 0};
     uint32_t init_blocks[4] = {0, 0, 0, 0};  // grids of the batched initialisation kernels
     cudaStream_t cap = nullptr;

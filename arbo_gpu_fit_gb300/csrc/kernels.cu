@@ -1179,7 +1179,8 @@ __global__ void __launch_bounds__(256, 4) k_demog_batch(BatchDev bd, uint32_t ko
 }
 
 // Force-of-infection pass of a batch: one warp per 32 consecutive (serotype, community) pairs of
-// an instance (bd.foi_off counts these warp items), in runs of bd.foi_run items per warp.
+// an instance (bd.foi_off counts these warp items), in runs of bd.foi_run items per warp. With
+// collect_only, only series row 0 of every instance (the end of its initialisation).
 __global__ void __launch_bounds__(512) k_foi_batch(BatchDev bd, int collect_only, uint32_t koff)
 {
     extern __shared__ __align__(16) unsigned char foi_dyn[];
