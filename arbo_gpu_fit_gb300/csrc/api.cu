@@ -1483,12 +1483,19 @@ int batch_configure(arbo_batch* b, const arbo_arch_param& a)
 // Re-uploads the descriptors of instances whose parameters changed (arbo_sim_set_param).
 int batch_refresh(arbo_batch* b)
 {
-    for (size_t i = 0; i < b->sims.size(); ++i) {
-        if (b->versions[i] == b->sims[i]->version) continue;
-        const Dev d = batch_desc(b, i);
-        CUDA_TRY(cudaMemcpy((Dev*)b->mem + i, &d, sizeof(Dev), cudaMemcpyHostToDevice));
-        b->versions[i] = b->sims[i]->version;
-    }
+    // One copy from the first to the last changed descriptor (an MCMC iteration changes them all).
+    const size_t n = b->sims.size();
+    size_t lo = n, hi = 0;
+    for (size_t i = 0; i < n; ++i)
+        if (b->versions[i] != b->sims[i]->version) {
+            lo = std::min(lo, i);
+            hi = i + 1;
+        }
+    if (lo >= hi) return ARBO_OK;
+    std::vector<Dev> devs(hi - lo);
+    for (size_t i = lo; i < hi; ++i) devs[i - lo] = batch_desc(b, i);
+    CUDA_TRY(cudaMemcpy((Dev*)b->mem + lo, devs.data(), sizeof(Dev) * (hi - lo), cudaMemcpyHostToDevice));
+    for (size_t i = lo; i < hi; ++i) b->versions[i] = b->sims[i]->version;
     return ARBO_OK;
 }
 
