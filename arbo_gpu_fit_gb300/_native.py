@@ -151,6 +151,7 @@ SIGNATURES = {
     "arbo_batch_destroy": (c_int, [c_void_p]),
     "arbo_batch_size": (c_int, [c_void_p, POINTER(c_uint32), POINTER(c_uint64)]),
     "arbo_batch_init": (c_int, [c_void_p, c_void_p]),
+    "arbo_batch_set_params": (c_int, [c_void_p, POINTER(SimParamStruct), POINTER(c_uint64), POINTER(c_uint32), c_void_p]),
     "arbo_batch_step": (c_int, [c_void_p, c_uint32, c_void_p]),
     "arbo_batch_run": (c_int, [c_void_p, c_void_p]),
     "arbo_batch_set_arch": (c_int, [c_void_p, POINTER(ArchParamStruct)]),

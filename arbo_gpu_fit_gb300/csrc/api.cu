@@ -613,11 +613,13 @@ int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* e, size_t n)
     return ARBO_OK;
 }
 
-int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p)
+}  // extern "C"
+
+// Why p may not replace the parameters of s (nullptr: it may). Sizes, life expectancies and table
+// ranges fix the allocation and the tables.
+static const char* param_change_error(const arbo_sim* s, const arbo_sim_param* p)
 {
-    if (!s || !p) return fail(ARBO_ERR_INVALID, "null argument");
     const arbo_sim_param& o = s->p;
-    // Sizes, life expectancies and table ranges fix the allocation and the tables.
     const bool same_shape = p->nSize == o.nSize && p->metaPop == o.metaPop && p->mSize == o.mSize &&
                             p->nStrains == o.nStrains && p->nShapeInfantMortality == o.nShapeInfantMortality &&
                             p->nScaleInfantMortality == o.nScaleInfantMortality &&
@@ -629,23 +631,38 @@ int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p)
                             p->recordSpatial == o.recordSpatial && p->nHeteroPopSize == o.nHeteroPopSize &&
                             p->mHeteroPopSize == o.mHeteroPopSize;
     if (!same_shape)
-        return fail(ARBO_ERR_INVALID, "arbo_sim_set_param changes only transmission, dispersal, seeding, seasonal "
-                                      "and attempt parameters; sizes and life expectancies need a new handle");
+        return "arbo_sim_set_param changes only transmission, dispersal, seeding, seasonal and attempt parameters; "
+               "sizes and life expectancies need a new handle";
     if (p->maxTargetAttempt < 1 || p->maxTargetAttempt > (1u << 18) || p->maxIntroAttempt > (1u << 26))
-        return fail(ARBO_ERR_INVALID, "attempt limits out of range");
-    if (const char* why = param_error(*p, s->d.N, s->d.M)) return fail(ARBO_ERR_INVALID, why);
-    CUDA_TRY(cudaSetDevice(s->device));
-    CUDA_TRY(cudaDeviceSynchronize());  // no step of this handle may be reading the old series
-    s->p = *p;
-    apply_rates(*p, s->d);
-    fill_expected(*p, s->d.M, s->d.T, s->etab);
-    CUDA_TRY(cudaMemcpy(s->d.etab, s->etab.data(), s->etab.size() * 4, cudaMemcpyHostToDevice));
-    s->h2d += s->etab.size() * 4;
-    // Captured graphs hold the old descriptor.
+        return "attempt limits out of range";
+    return param_error(*p, s->d.N, s->d.M);
+}
+
+// The host side of a parameter change (the device must be idle): rates in the descriptor, the
+// expected-mosquito series recomputed (the caller uploads s->etab), captured graphs dropped (they
+// hold the old descriptor), the descriptor version bumped for batches.
+static void param_change_host(arbo_sim* s, const arbo_sim_param& p)
+{
+    s->p = p;
+    apply_rates(p, s->d);
+    fill_expected(p, s->d.M, s->d.T, s->etab);
     if (s->gmulti) cudaGraphExecDestroy(s->gmulti);
     if (s->gone) cudaGraphExecDestroy(s->gone);
     s->gmulti = s->gone = nullptr;
     s->version += 1;
+}
+
+extern "C" {
+
+int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p)
+{
+    if (!s || !p) return fail(ARBO_ERR_INVALID, "null argument");
+    if (const char* why = param_change_error(s, p)) return fail(ARBO_ERR_INVALID, why);
+    CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // no step of this handle may be reading the old series
+    param_change_host(s, *p);
+    CUDA_TRY(cudaMemcpy(s->d.etab, s->etab.data(), s->etab.size() * 4, cudaMemcpyHostToDevice));
+    s->h2d += s->etab.size() * 4;
     return ARBO_OK;
 }
 
@@ -1312,6 +1329,8 @@ struct arbo_batch {
     void* mem = nullptr;  // Dev[n], then the phases' block tables, the work counter, the init block tables
     uint32_t blocks[3] = {0, 0, 0};
     uint32_t init_blocks[4] = {0, 0, 0, 0};  // grids of the batched initialisation kernels
+    void* stage = nullptr;                    // pinned staging of arbo_batch_set_params
+    size_t stage_bytes = 0;
     cudaStream_t cap = nullptr;
     cudaGraphExec_t gmulti = nullptr, gone = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1631,6 +1650,7 @@ int arbo_batch_destroy(arbo_batch* b)
     if (b->cap) cudaStreamDestroy(b->cap);
     if (b->flush) cudaFree(b->flush);
     if (b->mem) cudaFree(b->mem);
+    if (b->stage) cudaFreeHost(b->stage);
     delete b;
     return ARBO_OK;
 }
@@ -1680,6 +1700,57 @@ int arbo_batch_init(arbo_batch* b, void* stream)
         s->host_t = 0;
         s->inited = true;
     }
+    return ARBO_OK;
+}
+
+// arbo_sim_set_param and arbo_sim_set_seed for every instance at once: every change validated
+// before any is made, one device synchronisation, the expected-mosquito series and random keys
+// uploaded by asynchronous copies from one pinned staging buffer on `stream`.
+int arbo_batch_set_params(arbo_batch* b, const arbo_sim_param* params, const uint64_t* seeds,
+                          const uint32_t* instances, void* stream)
+{
+    if (!b || (!params && !seeds) || (instances && !seeds))
+        return fail(ARBO_ERR_INVALID, "arbo_batch_set_params: bad arguments");
+    const size_t n = b->sims.size();
+    if (params)
+        for (size_t i = 0; i < n; ++i)
+            if (const char* why = param_change_error(b->sims[i], &params[i]))
+                return fail(ARBO_ERR_INVALID, "arbo_batch_set_params, instance " + std::to_string(i) + ": " + why);
+    CUDA_TRY(cudaSetDevice(b->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // no step of any instance may be reading the old series
+    size_t bytes = seeds ? n * 16 : 0;
+    if (params)
+        for (const arbo_sim* s : b->sims) bytes += ((size_t)s->d.T + 1) * 4;
+    if (b->stage_bytes < bytes) {
+        if (b->stage) cudaFreeHost(b->stage);
+        b->stage = nullptr;
+        b->stage_bytes = 0;
+        CUDA_TRY(cudaMallocHost(&b->stage, bytes));
+        b->stage_bytes = bytes;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    char* at = (char*)b->stage;
+    for (size_t i = 0; i < n; ++i) {
+        arbo_sim* s = b->sims[i];
+        if (params) {
+            param_change_host(s, params[i]);
+            const size_t eb = s->etab.size() * 4;
+            std::memcpy(at, s->etab.data(), eb);
+            CUDA_TRY(cudaMemcpyAsync(s->d.etab, at, eb, cudaMemcpyHostToDevice, st));
+            s->h2d += eb;
+            at += eb;
+        }
+        if (seeds) {
+            s->seed = seeds[i];
+            s->instance = instances ? instances[i] : 0u;
+            const uint32_t kv[3] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32), s->instance};
+            std::memcpy(at, kv, sizeof(kv));
+            CUDA_TRY(cudaMemcpyAsync(&s->d.ctrl->k0, at, sizeof(kv), cudaMemcpyHostToDevice, st));
+            s->h2d += sizeof(kv);
+            at += 16;
+        }
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));  // the staging buffer is reused by the next call
     return ARBO_OK;
 }
 

@@ -162,6 +162,19 @@ class MCMC:
         check(self._lib.arbo_sim_set_param(sim._h, byref(sp)))
         sim.set_seed(sim_seed(self.workload.seed, chain, replicate, it))
 
+    def copy_params_batch(self, batch: Batch, theta, chains, it: int) -> None:
+        """copy_params for every handle of a batch in one call (Batch.set_params, one device
+        synchronisation): handle j * R + r takes the proposal theta[chains[j]] and the seed of
+        (chains[j], r, it)."""
+        params, seeds = [], []
+        for c in chains:
+            th = np.clip(np.asarray(theta[c], np.float64), self.lo, self.hi)
+            sp = configs.apply_theta(self.base, th)
+            for r in range(self.R):
+                params.append(sp)
+                seeds.append(sim_seed(self.workload.seed, int(c), r, it))
+        batch.set_params(params, seeds)
+
     def calc_log_likelihood(self, sims: List[Simulation], c0: int, c1: int, current: bool = False) -> None:
         hs = (c_void_p * len(sims))(*[s._h.value for s in sims])
         check(self._lib.arbo_mcmc_loglik(self._h, hs, int(c0), int(c1), int(current), None))
@@ -447,9 +460,7 @@ def start(m: MCMC, theta0: np.ndarray, sims: List[Simulation], batch: Optional[B
                 _simulate_alone(sims[r])
             m.calc_log_likelihood(sims[:m.R], c, c + 1, current=True)
     else:
-        for c in range(m.C):
-            for r in range(m.R):
-                m.copy_params(sims[c * m.R + r], theta0[c], c, r, 0)
+        m.copy_params_batch(batch, theta0, range(m.C), 0)
         batch.init()
         batch.run()
         m.calc_log_likelihood(sims, 0, m.C, current=True)
@@ -508,9 +519,7 @@ def run_batched(m: MCMC, iters: int, theta0: np.ndarray, sims: Optional[List[Sim
     sim_s = 0.0
     for it in range(it0, iters):
         prop = m.propose(it)
-        for c in range(m.C):
-            for r in range(m.R):
-                m.copy_params(sims[c * m.R + r], prop[c], c, r, it)
+        m.copy_params_batch(batch, prop, range(m.C), it)
         t1 = time.perf_counter()
         batch.init()
         batch.run()
@@ -561,9 +570,7 @@ def run_delayed(m: MCMC, iters: int, theta0: np.ndarray, surrogate: Callable[[np
                 if n not in batches:
                     batches[n] = chain_batch(sims[: n * m.R])
                 # Handle rows of the passing chains: the first n*R handles, in chain order.
-                for j, c in enumerate(passed):
-                    for r in range(m.R):
-                        m.copy_params(sims[j * m.R + r], prop[c], int(c), r, it)
+                m.copy_params_batch(batches[n], prop, passed, it)
                 t1 = time.perf_counter()
                 batches[n].init()
                 batches[n].run()

@@ -317,6 +317,24 @@ class Batch:
     def init(self) -> None:
         check(self._lib.arbo_batch_init(self._h, self.stream))
 
+    def set_params(self, params=None, seeds=None, instances=None) -> None:
+        """Parameters and/or seeds of every instance in one call (arbo_batch_set_params): the same
+        as Simulation.set_seed and arbo_sim_set_param per instance, with one device
+        synchronisation. params: one SimulationParam per instance; seeds, instances: one each."""
+        n = len(self.sims)
+        pa = sa = ia = None
+        if params is not None:
+            if len(params) != n:
+                raise ValueError(f"need {n} parameter sets, got {len(params)}")
+            pa = (SimParamStruct * n)(*params)
+        if seeds is not None:
+            sa = np.ascontiguousarray(np.asarray(seeds, np.uint64).reshape(n))
+        if instances is not None:
+            ia = np.ascontiguousarray(np.asarray(instances, np.uint32).reshape(n))
+        check(self._lib.arbo_batch_set_params(
+            self._h, pa, None if sa is None else sa.ctypes.data_as(POINTER(ctypes.c_uint64)),
+            None if ia is None else ia.ctypes.data_as(POINTER(c_uint32)), self.stream))
+
     def step(self, nsteps: int = 1) -> None:
         check(self._lib.arbo_batch_step(self._h, int(nsteps), self.stream))
 

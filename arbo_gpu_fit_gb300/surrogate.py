@@ -178,11 +178,9 @@ def training_set(workload: configs.Workload, n: int, months: int, seed: int = 0,
         with chain_batch(sims) as b:
             for i0 in range(0, n, len(sims)):
                 k = min(len(sims), n - i0)
-                for j in range(len(sims)):
-                    th = theta[min(i0 + j, n - 1)]
-                    sp = configs.apply_theta(w.parameter.simulation, th)
-                    check(load().arbo_sim_set_param(sims[j]._h, byref(sp)))
-                    sims[j].set_seed(sim_seed(w.seed ^ 0x5A5A, i0 + j, 0, 0))
+                b.set_params([configs.apply_theta(w.parameter.simulation, theta[min(i0 + j, n - 1)])
+                              for j in range(len(sims))],
+                             [sim_seed(w.seed ^ 0x5A5A, i0 + j, 0, 0) for j in range(len(sims))])
                 b.init()
                 b.run()
                 for j in range(k):

@@ -440,6 +440,15 @@ int arbo_batch_size(const arbo_batch* b, uint32_t* n, uint64_t* agents);
 /* arbo_sim_init of every instance, with the parameters and seeds the handles hold now; the same
  * results as initialising each alone, in five kernel launches for the whole batch. */
 int arbo_batch_init(arbo_batch* b, void* stream);
+/* arbo_sim_set_param(sims[i], &params[i]) and arbo_sim_set_seed(sims[i], seeds[i], instances[i])
+ * for every instance i, as MCMC::copyParams does before each proposal's simulations
+ * (cpp/MCMC.cpp:75-82), with one device synchronisation for the whole batch. params or seeds may
+ * be NULL (that part unchanged; not both); instances NULL: stream id 0 for every instance, as
+ * arbo_sim_set_seed(s, seed, 0). Every parameter change is validated before any is made
+ * (ARBO_ERR_INVALID naming the instance). Copies run on `stream`; the call returns once they are
+ * done. */
+int arbo_batch_set_params(arbo_batch* b, const arbo_sim_param* params, const uint64_t* seeds,
+                          const uint32_t* instances, void* stream);
 /* Advances every instance by nsteps (clamped to the shortest remaining run). */
 int arbo_batch_step(arbo_batch* b, uint32_t nsteps, void* stream);
 int arbo_batch_run(arbo_batch* b, void* stream);

@@ -47,6 +47,12 @@ def test_version(native):
     assert b"sm_103a" in native.arbo_version()
 
 
+def test_batch_setter_rejects_bad_arguments(native):
+    # Checked before any device call: no batch, or neither parameters nor seeds.
+    assert native.arbo_batch_set_params(None, None, None, None, None) == _native.ARBO_ERR_INVALID
+    assert b"arbo_batch_set_params" in native.arbo_last_error()
+
+
 def test_defaults_are_reference_constructor_values():
     p = SimulationParam()
     # cpp/SimulationParam.cpp:11-47

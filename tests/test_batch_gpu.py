@@ -71,19 +71,30 @@ def test_batch_equals_individual_steps(gpu, shape):
 def test_batch_reinit_equals_individual(gpu):
     # The batched initialisation after a run: new parameters and seeds (as an MCMC iteration sets
     # them), counters and series of the previous run cleared, every instance as if initialised alone.
+    # The handles stepped alone take them one call each (arbo_sim_set_param / arbo_sim_set_seed),
+    # the batch's in one arbo_batch_set_params.
     lib = _native.load()
     ws = workloads()
     alone, together = make(ws), make(ws)
     with Batch(together) as b:
         for run in range(3):
             if run:
-                for k, (x, y, w) in enumerate(zip(alone, together, ws)):
+                params = []
+                for k, (x, w) in enumerate(zip(alone, ws)):
                     sp = w.parameter.simulation.copy()
                     sp.bitingRate = sp.bitingRate * (0.8 if run == 1 else 1.1)
                     sp.externalInfection = sp.externalInfection * 0.5 * run
-                    for sim in (x, y):
-                        _native.check(lib.arbo_sim_set_param(sim._h, ctypes.byref(sp)))
-                        sim.set_seed(1000 * run + k, k)
+                    params.append(sp)
+                    _native.check(lib.arbo_sim_set_param(x._h, ctypes.byref(sp)))
+                    x.set_seed(1000 * run + k, k)
+                b.set_params(params, [1000 * run + k for k in range(len(ws))], list(range(len(ws))))
+                if run == 2:
+                    # All or nothing: with one bad parameter set (a changed size) no instance takes
+                    # the call's parameters or seeds (seed 7 would change every run compared below).
+                    bad = [p.copy() for p in params]
+                    bad[3].nSize = bad[3].nSize + 4
+                    with pytest.raises(_native.ArboError, match="instance 3"):
+                        b.set_params(bad, [7] * len(bad))
             for s in alone:
                 s.init()
             b.init()
