@@ -44,6 +44,32 @@ def test_sim_seed_distinct():
     assert len(seeds) == 8 * 3 * 50
 
 
+def test_batch_parameter_copy_matches_per_handle_copy():
+    # MCMC.copy_params_batch hands a batch the same parameters and seeds that copy_params gives each
+    # handle (handle j * R + r: chain chains[j], replicate r), including chains out of order (the
+    # delayed-acceptance driver passes the chains that passed the screen).
+    from types import SimpleNamespace
+
+    from arbo_gpu_fit_gb300.mcmc import MCMC
+
+    w = configs.scaled(600, 1800, 3, 60, seed=5)
+    box = configs.PRIOR_BOX
+    m = SimpleNamespace(R=3, base=w.parameter.simulation, workload=w,
+                        lo=np.array([b[1] for b in box]), hi=np.array([b[2] for b in box]))
+    theta = np.array([[0.5, 0.5, 0.9, 0.5, 100.0, 0.1], [0.3, 0.7, 0.8, 0.2, 200.0, 0.2],
+                      [2.0, -1.0, 0.95, 0.4, 50.0, 0.3]])  # the last one outside the box: clamped
+    got = {}
+    batch = SimpleNamespace(set_params=lambda params, seeds: got.update(params=params, seeds=seeds))
+    MCMC.copy_params_batch(m, batch, theta, [2, 0], it=7)
+    assert len(got["params"]) == len(got["seeds"]) == 6
+    for j, c in enumerate([2, 0]):
+        want = configs.apply_theta(w.parameter.simulation, np.clip(theta[c], m.lo, m.hi))
+        for r in range(3):
+            sp = got["params"][j * 3 + r]
+            assert bytes(sp) == bytes(want)
+            assert got["seeds"][j * 3 + r] == sim_seed(w.seed, c, r, 7)
+
+
 def test_serial_replay_is_deterministic_and_moves():
     w = configs.scaled(600, 1800, 3, 60, seed=5, sigma=0.3, bitingRate=0.9, nInitialInf=20.0, mInitialInf=60.0)
     obs = np.random.default_rng(1).integers(0, 30, (2, 4)).astype(np.uint32)
