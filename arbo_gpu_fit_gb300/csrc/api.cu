@@ -602,6 +602,7 @@ int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* e, size_t n)
 {
     if (!s || !e || n != (size_t)s->d.T + 1) return fail(ARBO_ERR_INVALID, "expected series must have max_time+1 entries");
     CUDA_TRY(cudaSetDevice(s->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // no step of this handle may be reading the old series
     for (size_t t = 0; t < n; ++t) {
         float v = e[t];
         if (v > (float)s->d.M) v = (float)s->d.M;

@@ -257,14 +257,17 @@ int arbo_sim_destroy(arbo_sim* s);
 
 /* Replace the expected mosquito population series E[0..max_time] (n = max_time+1 floats,
  * host memory). Default: the seasonal target of arbo_sim_param. Replaces the host array
- * h_mExpectedPopSize of cpp/simulation.cpp:84-132. Values above mSize are capped. */
+ * h_mExpectedPopSize of cpp/simulation.cpp:84-132. Values above mSize are capped. Synchronises
+ * the device. A later arbo_sim_set_param / arbo_batch_set_params recomputes the seasonal target. */
 int arbo_sim_set_expected_mosquitoes(arbo_sim* s, const float* expected, size_t n);
 
 /* Changes the parameters of an existing handle between runs, as MCMC::copyParams does before each
  * proposal's simulations (cpp/MCMC.cpp:75-82, cpp/main.cpp:96): transmission, dispersal, seeding,
  * recovery and latency, seasonal expected-mosquito and attempt parameters. Sizes, life
- * expectancies and table ranges must stay as created (ARBO_ERR_INVALID otherwise). Synchronises
- * the device; takes effect at the next arbo_sim_init / step (batches pick it up as well). */
+ * expectancies and table ranges must stay as created (ARBO_ERR_INVALID otherwise). Recomputes the
+ * expected-mosquito series from the seasonal parameters (replacing one set by
+ * arbo_sim_set_expected_mosquitoes). Synchronises the device; takes effect at the next
+ * arbo_sim_init / step (batches pick it up as well). */
 int arbo_sim_set_param(arbo_sim* s, const arbo_sim_param* p);
 
 /* Re-seed the handle (next arbo_sim_init uses it). */
