@@ -246,8 +246,10 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     }
     for (uint32_t mo = 0; mo < cfg->months; ++mo)
         if (cfg->month_start[mo + 1] < cfg->month_start[mo]) return mfail(ARBO_ERR_INVALID, "month_start not ascending");
+    int device = 0;
+    MCUDA(cudaGetDevice(&device));
     arbo_mcmc* h = new arbo_mcmc();
-    MCUDA(cudaGetDevice(&h->device));
+    h->device = device;
     McmcDev& m = h->m;
     m.C = C;
     m.D = D;
@@ -266,7 +268,7 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     const size_t n_cd = al((size_t)C * D * 8), n_c8 = al((size_t)C * 8), n_cr = al((size_t)C * R * 8);
     const size_t n_c4 = al((size_t)C * 4), n_c1 = al(C), n_ch = al((size_t)m.iters * C * D * 8 + 8);
     const size_t n_fl = al((size_t)m.iters * C + 1), n_refs = al((size_t)C * R * sizeof(SeriesRef));
-    const size_t total = n_d + n_y + n_mr + 2 * n_cd + 5 * n_c8 + n_cr + 2 * n_c4 + n_c1 + n_ch + n_fl + n_refs;
+    const size_t total = n_d + n_y + n_mr + 2 * n_cd + 4 * n_c8 + n_cr + 2 * n_c4 + n_c1 + n_ch + n_fl + n_refs;
     if (cudaMalloc(&h->mem, total) != cudaSuccess) {
         delete h;
         return mfail(ARBO_ERR_ALLOC, "arbo_mcmc_create: cudaMalloc of " + std::to_string(total) + " bytes");
@@ -292,8 +294,6 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     m.loglik = (double*)take(n_c8);
     m.screen = (double*)take(n_c8);
     m.screen_cur = (double*)take(n_c8);
-    double* spare = (double*)take(n_c8);
-    (void)spare;
     m.particle = (double*)take(n_cr);
     m.accepted = (uint32_t*)take(n_c4);
     m.passed = (uint32_t*)take(n_c4);
@@ -315,7 +315,7 @@ int arbo_mcmc_create(const arbo_mcmc_config* cfg, arbo_mcmc** out)
     if (cudaMemcpy(box, hb.data(), 3 * D * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy((void*)m.y, cfg->observed, (size_t)m.Mo * m.S * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy((void*)m.mrow, cfg->month_start, (m.Mo + 1) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(m.theta, 0, 2 * n_cd + 5 * n_c8 + n_cr + 2 * n_c4 + n_c1) != cudaSuccess)
+        cudaMemset(m.theta, 0, 2 * n_cd + 4 * n_c8 + n_cr + 2 * n_c4 + n_c1) != cudaSuccess)
         return bail("upload");
     std::vector<double> ninf(C, -INFINITY);
     if (cudaMemcpy(m.logpost, ninf.data(), C * 8, cudaMemcpyHostToDevice) != cudaSuccess) return bail("upload");
