@@ -134,3 +134,24 @@ def test_rhat():
     drifting = mixed + np.linspace(0, 5, 2000)[:, None, None]  # split halves disagree: about 1.45
     assert np.all(rhat(drifting) > 1.3)
     assert np.all(np.isnan(rhat(mixed[:3])))
+
+
+def test_fit_summary_and_adaptation_choice():
+    from arbo_gpu_fit_gb300 import fit
+
+    rng = np.random.default_rng(6)
+    chain = rng.standard_normal((300, 8, 3)) + np.array([1.0, 2.0, 3.0])
+    s = fit.summarize(chain, minutes=2.0, burn=100)
+    assert s["iters"] == 300 and s["kept"] == 200
+    assert np.allclose(s["mean"], [1.0, 2.0, 3.0], atol=0.05)
+    assert s["ess_per_min"] == pytest.approx(s["ess_min"] / 2.0)
+    assert s["rhat_max"] < 1.05
+    saved = fit.COV_START[0]
+    try:
+        fit.COV_START[0] = 0
+        assert fit.adaptation(50).cov is None
+        fit.COV_START[0] = 20
+        ad = fit.adaptation(50)
+        assert ad.cov.start == 20 and ad.cov.until == 50 and ad.step.until == 50
+    finally:
+        fit.COV_START[0] = saved
